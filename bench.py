@@ -1,0 +1,561 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 oneSolver hot paths; prints one JSON line.
+
+Workloads (--workload):
+  exhaustive36  Exhaustive search on a dense QUBO with n = 36 and integer
+                coefficients drawn uniformly from [-8, 8] (seed 0): 2^36
+                states, int32 Gray-code enumeration, ground energy and all
+                degenerate minimisers. Metric: enumerated states/s. (default)
+  sa-chimera    Sparse SA on a 16x16 Chimera of K4,4 cells (2048 spins),
+                J in {-1,+1}, h = 0, converted to QUBO; 1024 trajectories x
+                10,000 sweeps, linear beta 0.1 -> 3.0, FP32 fields with an
+                FP64 resync every 256 sweeps. Metric: spin-flip attempts/s.
+  sa-sk         Dense SA on a Sherrington-Kirkpatrick QUBO, n = 1024,
+                J_ij ~ N(0, 1/n); 512 trajectories x 1,000 sweeps, geometric
+                beta 0.1 -> 5.0. Metric: spin-flip attempts/s.
+  sa-n64        Dense SA, n = 64, N(0,1) entries (seed 0), 100 trajectories x
+                100 random-site steps, geometric beta 0.1 -> 1.0 with the
+                reference's acceptance rule. Metric: spin-flip attempts/s.
+
+A "step" is one whole pass of the workload (every state, or every sweep of
+every trajectory). `value` is timed on the device with CUDA events around the
+library's kernels (inputs resident in HBM, L2 flushed between steps); `e2e`
+times the reference-facing call with host buffers (upload, kernels, download).
+--impl reference times the reference algorithm (the oracle's CPU restatement)
+on the host cores instead.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+if str(ROOT) not in sys.path:
+    sys.path.insert(0, str(ROOT))
+
+L2_FLUSH_BYTES = 256 << 20     # > 129 MB L2
+
+
+# ---------------------------------------------------------------------------
+# Workload generators (seeded synthetic instances with the configs' shapes)
+# ---------------------------------------------------------------------------
+
+def int_qubo(n: int, seed: int, lo: int = -8, hi: int = 8) -> np.ndarray:
+    rng = np.random.default_rng(seed)
+    u = np.triu(rng.integers(lo, hi + 1, size=(n, n)).astype(np.float64))
+    return u + np.triu(u, 1).T
+
+
+def normal_qubo(n: int, seed: int, scale: float = 1.0) -> np.ndarray:
+    rng = np.random.default_rng(seed)
+    u = np.triu(rng.normal(0.0, scale, size=(n, n)))
+    return u + np.triu(u, 1).T
+
+
+def sk_qubo(n: int, seed: int) -> np.ndarray:
+    """SK Ising J_ij ~ N(0, 1/n), h = 0 -> QUBO (x = (s+1)/2, offset dropped)."""
+    rng = np.random.default_rng(seed)
+    J = np.triu(rng.normal(0.0, 1.0 / math.sqrt(n), size=(n, n)), 1)
+    Js = J + J.T
+    f = 4.0 * Js
+    np.fill_diagonal(f, -2.0 * Js.sum(axis=1))
+    return f
+
+
+def chimera_csr(L: int, seed: int):
+    """L x L Chimera (K4,4 cells), J in {-1,+1}, h = 0 -> QUBO in CSR form."""
+    import onesolver_gb300 as osg
+    rng = np.random.default_rng(seed)
+    n = 8 * L * L
+    rows, cols = [], []
+
+    def idx(r, c, side, k):
+        return (r * L + c) * 8 + side * 4 + k
+
+    for r in range(L):
+        for c in range(L):
+            for a in range(4):
+                for b in range(4):
+                    rows.append(idx(r, c, 0, a)); cols.append(idx(r, c, 1, b))
+            if r + 1 < L:
+                for k in range(4):
+                    rows.append(idx(r, c, 0, k)); cols.append(idx(r + 1, c, 0, k))
+            if c + 1 < L:
+                for k in range(4):
+                    rows.append(idx(r, c, 1, k)); cols.append(idx(r, c + 1, 1, k))
+    J = rng.choice([-1.0, 1.0], size=len(rows))
+    rows = np.array(rows); cols = np.array(cols)
+    diag = np.zeros(n)
+    np.add.at(diag, rows, -2.0 * J)
+    np.add.at(diag, cols, -2.0 * J)
+    r2 = np.concatenate([rows, cols]); c2 = np.concatenate([cols, rows]); v2 = np.concatenate([4 * J, 4 * J])
+    order = np.lexsort((c2, r2))
+    r2, c2, v2 = r2[order], c2[order], v2[order]
+    rp = np.zeros(n + 1, dtype=np.int32)
+    np.add.at(rp, r2 + 1, 1)
+    rp = np.cumsum(rp).astype(np.int32)
+    return osg.Csr(n, rp, c2.astype(np.int32), v2.astype(np.float64), diag)
+
+
+# ---------------------------------------------------------------------------
+# Clocks during the timed region
+# ---------------------------------------------------------------------------
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines: list[str] = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict | None:
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.thread.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for name, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# Distributed plumbing (one rank per GPU; replicas of independent instances)
+# ---------------------------------------------------------------------------
+
+def dist_setup(n_gpus: int):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        if backend == "nccl":
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend)
+        pg = dist
+    return world, rank, local, pg
+
+
+def barrier(pg):
+    if pg is not None:
+        pg.barrier()
+
+
+def max_over_ranks(pg, value: float) -> float:
+    if pg is None:
+        return value
+    import torch
+    dev = "cuda" if torch.cuda.is_available() else "cpu"
+    t = torch.tensor([value], dtype=torch.float64, device=dev)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+def load_peaks() -> dict:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        return json.loads(p.read_text())
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "fallback": True}
+
+
+# ---------------------------------------------------------------------------
+# Our implementation
+# ---------------------------------------------------------------------------
+
+def timed_steps(ctx_stream_setter, flush, run_one, kernel_ms, steps: int, warmup: int, pg):
+    """W untimed warm-up steps, then K timed steps with an L2 flush before
+    each; returns (per-step device ms list, per-step kernel ms list)."""
+    import torch
+    for _ in range(warmup):
+        run_one()
+    torch.cuda.synchronize()
+    barrier(pg)
+    torch.cuda.synchronize()
+    step_ms, kern_ms = [], []
+    for _ in range(steps):
+        flush()
+        s = torch.cuda.Event(enable_timing=True)
+        e = torch.cuda.Event(enable_timing=True)
+        s.record()
+        run_one()
+        e.record()
+        e.synchronize()
+        step_ms.append(s.elapsed_time(e))
+        kern_ms.append(kernel_ms())
+    torch.cuda.synchronize()
+    barrier(pg)
+    return step_ms, kern_ms
+
+
+def bench_exhaustive(args, ctx, pg, rank, world):
+    import torch
+    import onesolver_gb300 as osg
+    n = 36
+    f = int_qubo(n, rank)  # seed 0 on rank 0; independent instances on replicas
+    plan = osg.ExhaustivePlan(f, ctx=ctx, max_minimisers=1 << 16)
+    flush_buf = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+    launches = []
+
+    def run_one():
+        plan.execute()
+        launches.append(plan.launches)
+
+    sampler = ClockSampler(torch.cuda.current_device())
+    for _ in range(args.warmup):
+        run_one()
+    torch.cuda.synchronize()
+    sampler.start()
+    launches.clear()
+    step_ms, kern_ms = timed_steps(None, lambda: flush_buf.zero_(), run_one, plan.kernel_ms, args.steps, 0, pg)
+    clocks = sampler.stop()
+    res = plan.result()
+    states = float(1 << n)
+    t_step = max_over_ranks(pg, sum(step_ms) / len(step_ms))
+    value = world * states / (t_step * 1e-3)
+
+    # End to end: the reference-facing call with host buffers (upload, kernels, download).
+    torch.cuda.synchronize()
+    e2e_t = []
+    for i in range(max(3, args.steps // 5)):
+        t0 = time.perf_counter()
+        r = osg.exhaustive(f, ctx=ctx, max_minimisers=1 << 16)
+        e2e_t.append(time.perf_counter() - t0)
+    assert r.energy == res.energy and r.count == res.count
+    e2e_step = max_over_ranks(pg, statistics.mean(e2e_t))
+    h2d = n * n * 4 + 512 * 4
+    d2h = 56 + 8 * min(r.count, 1 << 16)
+
+    k_ms = statistics.mean(kern_ms)
+    peak = osg.probe_int32_peak(ctx)
+    achieved = states * 2 / (k_ms * 1e-3) / 1e9
+    out = {
+        "metric": "exhaustive enumerated states/s (n=36, int32 Gray code, all degenerate minimisers)",
+        "value": value, "unit": "states/s", "ms_per_step": t_step,
+        "dtype": "int32",
+        "config": {"workload": "exhaustive search, dense QUBO n=36, integer Q_ij ~ U{-8..8} (seed 0), "
+                               "2^36 states, ground energy + all degenerate minimisers",
+                   "n": n, "states_per_step": int(states), "l2": "flushed (256 MB write) before every timed step",
+                   "parallelism": f"replicas x{world}" if world > 1 else "1 GPU"},
+        "result": {"energy": res.energy, "state": res.state, "minimisers": res.count},
+        "roofline": {"bound": "int32-issue", "achieved": achieved, "peak": peak, "unit": "Gop/s",
+                     "frac": achieved / peak, "traffic": TRAFFIC.get("exhaustive36"),
+                     "ops_per_unit": 2, "kernel_ms": k_ms,
+                     "peak_source": "os_probe_int32_peak: add+min issue rate measured in this run "
+                                    "(MEASURED_PEAKS.json has no INT32 figure)"},
+        "e2e": {"value": world * states / e2e_step, "unit": "states/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h, "ms_per_step": e2e_step * 1e3},
+        "gpu_launches": int(sum(launches)),
+        "clocks": clocks,
+    }
+    plan.close()
+    return out
+
+
+def bench_sa(args, ctx, pg, rank, world, workload):
+    import torch
+    import onesolver_gb300 as osg
+    if workload == "sa-chimera":
+        q = chimera_csr(16, rank)
+        n, T = q.n, 1024
+        beta = osg.linear_schedule(0.1, 2.9, 10000)  # reference linear form: ends at 0.1 + 2.9 = 3.0
+        plan = osg.AnnealPlan(q, beta, num_tries=T, resync_every=256, acceptance=osg.ACCEPT_PHYSICAL, ctx=ctx)
+        desc = ("sparse SA, 16x16 Chimera (K4,4 cells), 2048 spins, J in {-1,+1}, h=0 -> QUBO; 1024 "
+                "trajectories x 10,000 sweeps, linear beta 0.1->3.0, FP32 fields, FP64 resync every 256 sweeps")
+        attempts = T * 10000 * n
+        h2d = (q.row_ptr.nbytes + q.col.nbytes + q.val.nbytes + q.diag.nbytes + beta.nbytes)
+        upload = lambda: osg.anneal_sparse(q, beta, num_tries=T, resync_every=256, acceptance=osg.ACCEPT_PHYSICAL,
+                                           ctx=ctx)
+        fmas_per_attempt = float(q.row_ptr[-1]) / n  # neighbours updated per accepted flip
+    elif workload == "sa-sk":
+        n, T = 1024, 512
+        f = sk_qubo(n, rank)
+        beta = osg.geometric_schedule(0.1, 5.0, 1000)
+        plan = osg.AnnealPlan(f, beta, num_tries=T, resync_every=250, acceptance=osg.ACCEPT_PHYSICAL,
+                              site_order=osg.SITES_SEQUENTIAL, ctx=ctx)
+        desc = ("dense SA, SK n=1024 J~N(0,1/n) -> QUBO; 512 trajectories x 1,000 sweeps, geometric beta "
+                "0.1->5.0, FP32 fields, FP64 resync every 250 sweeps")
+        attempts = T * 1000 * n
+        h2d = f.nbytes + beta.nbytes
+        upload = lambda: osg.anneal(f, beta, num_tries=T, resync_every=250, acceptance=osg.ACCEPT_PHYSICAL,
+                                    site_order=osg.SITES_SEQUENTIAL, ctx=ctx)
+        fmas_per_attempt = float(n)
+    else:  # sa-n64
+        n, T = 64, 100
+        f = normal_qubo(n, rank)
+        beta = osg.geometric_schedule(0.1, 1.0, 100)
+        plan = osg.AnnealPlan(f, beta, num_tries=T, acceptance=osg.ACCEPT_REFERENCE, site_order=osg.SITES_RANDOM,
+                              ctx=ctx)
+        desc = ("dense SA, n=64, N(0,1) entries (seed 0); 100 trajectories x 100 random-site steps, geometric "
+                "beta 0.1->1.0, reference acceptance (the reference CLI's default run)")
+        attempts = T * 100
+        h2d = f.nbytes + beta.nbytes
+        upload = lambda: osg.anneal(f, beta, num_tries=T, ctx=ctx)
+        fmas_per_attempt = float(n)
+    flush_buf = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+    launches = []
+
+    def run_one():
+        plan.execute()
+        launches.append(plan.launches)
+
+    for _ in range(args.warmup):
+        run_one()
+    torch.cuda.synchronize()
+    sampler = ClockSampler(torch.cuda.current_device())
+    sampler.start()
+    launches.clear()
+    steps = args.steps
+    step_ms, kern_ms = timed_steps(None, lambda: flush_buf.zero_(), run_one, plan.kernel_ms, steps, 0, pg)
+    clocks = sampler.stop()
+    res = plan.result()
+    t_step = max_over_ranks(pg, statistics.mean(step_ms))
+    value = world * attempts / (t_step * 1e-3)
+    e2e_t = []
+    for _ in range(max(2, steps // 5)):
+        t0 = time.perf_counter()
+        r = upload()
+        e2e_t.append(time.perf_counter() - t0)
+    e2e_step = max_over_ranks(pg, statistics.mean(e2e_t))
+    k_ms = statistics.mean(kern_ms)
+    peak = osg.probe_fp32_fma_peak(ctx)
+    acc_rate = res.accepted / max(res.attempts, 1)
+    # Algorithmic FP32 FMAs: every accepted flip updates its row of fields.
+    achieved = res.accepted * fmas_per_attempt * 2 / (k_ms * 1e-3) / 1e9
+    out = {
+        "metric": "SA spin-flip attempts/s",
+        "value": value, "unit": "attempts/s", "ms_per_step": t_step, "dtype": "fp32",
+        "config": {"workload": desc, "n": n, "trajectories": T, "attempts_per_step": attempts,
+                   "l2": "flushed (256 MB write) before every timed step",
+                   "parallelism": f"replicas x{world}" if world > 1 else "1 GPU"},
+        "result": {"best_energy": res.energy, "acceptance_rate": acc_rate, "max_field_drift": res.max_field_drift},
+        "roofline": {"bound": "fp32-fma", "achieved": achieved, "peak": peak, "unit": "GFLOP/s",
+                     "frac": achieved / peak, "traffic": TRAFFIC.get(workload), "kernel_ms": k_ms,
+                     "kernel_attempts_per_s": attempts / (k_ms * 1e-3),
+                     "peak_source": "os_probe_fp32_fma_peak measured in this run"},
+        "e2e": {"value": world * attempts / e2e_step, "unit": "attempts/s", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(n * T + 8 * T + 8 * 3), "ms_per_step": e2e_step * 1e3},
+        "gpu_launches": int(sum(launches)),
+        "clocks": clocks,
+    }
+    plan.close()
+    return out
+
+
+# DRAM bytes per launch of the dominant kernel, from the ncu captures
+# summarised under profiles/ (null until captured).
+TRAFFIC: dict = {}
+
+
+# ---------------------------------------------------------------------------
+# CPU baselines (the reference's algorithm, restated in oracle/)
+# ---------------------------------------------------------------------------
+
+def cpu_exhaustive_rate(f: np.ndarray, budget_s: float, threads: int) -> tuple[float, int, float]:
+    import oracle
+    oracle.build()
+    n = f.shape[0]
+    t0 = time.perf_counter()
+    probe = 1 << 16
+    oracle.exhaustive(f, 0, probe, threads)
+    rate = probe / max(time.perf_counter() - t0, 1e-6)
+    sample = int(min(1 << n, max(probe, 2 ** int(math.log2(rate * budget_s)))))
+    t0 = time.perf_counter()
+    oracle.exhaustive(f, 0, sample, threads)
+    dt = time.perf_counter() - t0
+    return sample / dt, sample, dt
+
+
+def cpu_sa_rate(workload: str, budget_s: float, threads: int):
+    """Reference algorithm (full FP64 energy per attempt) on a bounded sample."""
+    import oracle
+    import onesolver_gb300 as osg
+    oracle.build()
+    if workload == "sa-chimera":
+        f = chimera_csr(16, 0).to_dense()
+        order, acc = 1, 1
+        beta = osg.linear_schedule(0.1, 2.9, 10000)
+    elif workload == "sa-sk":
+        f = sk_qubo(1024, 0)
+        order, acc = 1, 1
+        beta = osg.geometric_schedule(0.1, 5.0, 1000)
+    else:
+        f = normal_qubo(64, 0)
+        order, acc = 0, 0
+        beta = osg.geometric_schedule(0.1, 1.0, 100)
+    n = f.shape[0]
+    # One step of `threads` trajectories, growing until the budget is used.
+    iters = 1
+    while True:
+        t0 = time.perf_counter()
+        _, _, att = oracle.anneal_free(f, beta[:iters], threads, 1, 1, acc, order, threads)
+        dt = time.perf_counter() - t0
+        if dt > budget_s / 4 or iters >= len(beta):
+            break
+        iters = min(len(beta), iters * 4)
+    return att / dt, f"{threads} trajectories x {iters} steps ({att} attempts) of the same instance", dt
+
+
+def reference_arm(args, world, rank):
+    """--impl reference: the reference's algorithm on the host cores."""
+    if rank != 0:
+        return None
+    threads = os.cpu_count() or 1
+    w = args.workload
+    vals = []
+    sample_desc = ""
+    for i in range(args.warmup + args.steps):
+        if w == "exhaustive36":
+            rate, sample, dt = cpu_exhaustive_rate(int_qubo(36, 0), min(10.0, args.ref_budget), threads)
+            sample_desc = (f"states [0, {sample}) of the n=36 instance per step, reference O(n^2) FP64 loop "
+                           f"(include/exhaustive/exhaustive.hpp:110-134)")
+        else:
+            rate, sample_desc, dt = cpu_sa_rate(w, min(10.0, args.ref_budget), threads)
+        if i >= args.warmup:
+            vals.append(rate)
+    value = statistics.mean(vals)
+    unit = "states/s" if w == "exhaustive36" else "attempts/s"
+    return {"impl": "reference", "metric": METRICS[w], "value": value, "unit": unit, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": CONFIG_NAMES[w]},
+            "cpu_baseline": {"value": value, "unit": unit, "cores": threads, "kind": "port", "sample": sample_desc},
+            "e2e": {"value": value, "unit": unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+METRICS = {
+    "exhaustive36": "exhaustive enumerated states/s (n=36, int32 Gray code, all degenerate minimisers)",
+    "sa-chimera": "SA spin-flip attempts/s",
+    "sa-sk": "SA spin-flip attempts/s",
+    "sa-n64": "SA spin-flip attempts/s",
+}
+CONFIG_NAMES = {
+    "exhaustive36": "exhaustive search, dense QUBO n=36, integer Q_ij ~ U{-8..8} (seed 0), 2^36 states",
+    "sa-chimera": "sparse SA, 16x16 Chimera 2048 spins, 1024 trajectories x 10,000 sweeps",
+    "sa-sk": "dense SA, SK n=1024, 512 trajectories x 1,000 sweeps",
+    "sa-n64": "dense SA, n=64, 100 trajectories x 100 steps (reference CLI defaults)",
+}
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=0, help="timed steps (default per workload)")
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=list(METRICS), default="exhaustive36")
+    ap.add_argument("--secondary", action=argparse.BooleanOptionalAction, default=True,
+                    help="also measure the SA workloads and report them under 'secondary'")
+    ap.add_argument("--cpu-baseline", action=argparse.BooleanOptionalAction, default=True)
+    ap.add_argument("--ref-budget", type=float, default=8.0, help="seconds of CPU work per reference step")
+    args = ap.parse_args()
+    if args.steps <= 0:
+        args.steps = {"exhaustive36": 50, "sa-chimera": 10, "sa-sk": 5, "sa-n64": 50}[args.workload]
+    args.warmup = max(args.warmup, 3)
+
+    world, rank, local, pg = dist_setup(args.gpus)
+    if args.impl == "reference":
+        out = reference_arm(args, world, rank)
+        if out is not None:
+            print(json.dumps(out))
+        return
+
+    import torch
+    import onesolver_gb300 as osg
+    torch.cuda.set_device(local)
+    ctx = osg.Context(local)
+    ctx.set_stream(torch.cuda.current_stream().cuda_stream)
+
+    if args.workload == "exhaustive36":
+        out = bench_exhaustive(args, ctx, pg, rank, world)
+    else:
+        out = bench_sa(args, ctx, pg, rank, world, args.workload)
+
+    if args.secondary and args.workload == "exhaustive36":
+        sec = {}
+        for w, k in (("sa-chimera", 3), ("sa-sk", 3)):
+            a2 = argparse.Namespace(**vars(args))
+            a2.steps, a2.warmup = k, 3
+            r = bench_sa(a2, ctx, pg, rank, world, w)
+            sec[w] = {"value": r["value"], "unit": r["unit"], "config": r["config"]["workload"],
+                      "kernel_attempts_per_s": r["roofline"]["kernel_attempts_per_s"],
+                      "roofline": {k2: r["roofline"][k2] for k2 in ("bound", "achieved", "peak", "unit", "frac")},
+                      "e2e": r["e2e"]["value"], "result": r["result"], "gpu_launches": r["gpu_launches"]}
+        out["secondary"] = sec
+
+    if rank == 0 and world == 1 and args.cpu_baseline:
+        threads = os.cpu_count() or 1
+        if args.workload == "exhaustive36":
+            rate, sample, dt = cpu_exhaustive_rate(int_qubo(36, 0), 15.0, threads)
+            out["cpu_baseline"] = {"value": rate, "unit": "states/s", "cores": threads, "kind": "port",
+                                   "sample": f"states [0, {sample}) of the same n=36 instance ({dt:.1f} s), "
+                                             f"reference O(n^2) FP64 loop on {threads} threads"}
+        else:
+            rate, desc, dt = cpu_sa_rate(args.workload, 15.0, threads)
+            out["cpu_baseline"] = {"value": rate, "unit": "attempts/s", "cores": threads, "kind": "port",
+                                   "sample": desc + f" ({dt:.1f} s), full FP64 energy per attempt"}
+
+    if rank == 0:
+        line = {"metric": out["metric"], "value": out["value"], "unit": out["unit"], "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": out["ms_per_step"],
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": out["dtype"],
+                "data": "synthetic (seeded; shapes and distributions of the configs)", "config": out["config"]}
+        for k in ("roofline", "cpu_baseline", "e2e", "gpu_launches", "clocks", "result", "secondary"):
+            if k in out:
+                line[k] = out[k]
+        print(json.dumps(line))
+    ctx.close()
+    if pg is not None:
+        pg.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

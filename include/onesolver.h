@@ -1,0 +1,325 @@
+/* onesolver.h -- C ABI of the GB300 (sm_103a) oneSolver backend.
+ *
+ * This is the drop-in boundary for oneSolver's two hot paths. The reference
+ * (quantumz-io/oneSolver) has no FFI layer; its boundary is the C++ template
+ * API plus two CLIs. Each entry point below names the reference function it
+ * replaces (paths relative to the reference project root). The C++ mirror of
+ * the reference API (include/onesolver/*.hpp: qubo::QUBOModel, sa::anneal,
+ * exhaustive::solve, devices::construct_device_selector) is written on top of
+ * these functions, and so are the CLIs.
+ *
+ * Conventions
+ *   - Every function returns an os_status; no C++ exception crosses the ABI.
+ *     On failure os_last_error() (thread-local) holds a human-readable reason.
+ *   - The caller owns every host buffer. Device memory lives inside an
+ *     os_ctx (or a plan created from one) and is freed with it.
+ *   - Calls are synchronous unless the name says "execute" (those only
+ *     enqueue work on the given stream).
+ *   - A dense QUBO is the reference's flattened matrix
+ *     (helpers::flatten_qubo, include/helpers/qubo_helpers.hpp:26-44):
+ *     n*n doubles, row-major, diagonal = linear terms. Only the upper
+ *     triangle (i <= j) is read, exactly as both reference energy functions
+ *     read it (annealing.hpp:31-40, exhaustive.hpp:44-61), so a symmetric or
+ *     an upper-triangular matrix gives the same result.
+ *   - Exhaustive states are uint64 with bit i = variable i
+ *     (helpers::ulong_to_vec, include/helpers/ulong_to_vec.hpp:23-32).
+ */
+#ifndef ONESOLVER_H_
+#define ONESOLVER_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define OS_ABI_VERSION 1
+
+typedef enum os_status {
+  OS_OK = 0,
+  OS_INVALID_ARG = 1,          /* bad argument; reference: std::invalid_argument */
+  OS_CUDA_ERROR = 2,           /* CUDA runtime error; reference: sycl::exception */
+  OS_TIMEOUT = 3,              /* a bounded device wait ran out */
+  OS_OVERFLOW_MINIMISERS = 4,  /* more minimisers than the caller's buffer holds */
+  OS_NO_DEVICE = 5,            /* no CUDA device of the requested index */
+  OS_PARSE_ERROR = 6,          /* .qubo text rejected (qubo.hpp:313-314,355-373,413-415) */
+  OS_UNSUPPORTED = 7           /* e.g. --device-type host/cpu: this build has no CPU backend */
+} os_status;
+
+/* ------------------------------------------------------------------------ */
+/* Library, errors, devices                                                 */
+/* ------------------------------------------------------------------------ */
+
+/* ABI version of the loaded library (OS_ABI_VERSION). No reference counterpart. */
+int32_t os_abi_version(void);
+
+/* Detail of the last failure on this thread. Reference: the what() string of
+ * the exception thrown (annealing.hpp:128-132, qubo.hpp:313-415). */
+const char *os_last_error(void);
+
+/* Short name of a status code. */
+const char *os_status_string(os_status status);
+
+/* Device selection by the reference's --device-type string. Replaces
+ * devices::construct_device_selector (include/helpers/devices.hpp:27-42):
+ * "gpu" -> CUDA device 0; "cpu" and "host" -> OS_UNSUPPORTED (this build
+ * has no CPU backend and never falls back to one); anything else ->
+ * OS_INVALID_ARG with "Unknown device type: <s>". */
+os_status os_select_device(const char *device_type, int32_t *device_out);
+
+/* Device name for the CLIs' "Using device:" line
+ * (app/one-solver-anneal.cpp:149-151). */
+os_status os_device_name(int32_t device, char *buf, size_t cap);
+
+/* Execution context: one CUDA device, one stream, cached device buffers.
+ * Replaces the sycl::queue the reference passes to its solvers
+ * (app/one-solver-anneal.cpp:139-147). */
+typedef struct os_ctx os_ctx;
+os_status os_ctx_create(int32_t device, os_ctx **out);
+os_status os_ctx_destroy(os_ctx *ctx);
+/* Use a caller-owned cudaStream_t (passed as void*) instead of the
+ * context's own stream; NULL restores the context's stream. */
+os_status os_ctx_set_stream(os_ctx *ctx, void *stream);
+
+/* ------------------------------------------------------------------------ */
+/* Model and file IO (host only; no GPU needed)                             */
+/* ------------------------------------------------------------------------ */
+
+/* Parsed QUBO model. Replaces qubo::QUBOModel<int,double> as produced by
+ * QUBOModel::load (include/model/qubo.hpp:425-430) through parse_qubo
+ * (qubo.hpp:392-417) and QUBOBuilder (qubo.hpp:282-379). */
+typedef struct os_model os_model;
+
+/* Parse .qubo text with the reference grammar and validation. Errors are
+ * OS_PARSE_ERROR with the reference's message in os_last_error(). */
+os_status os_model_parse(const char *text, size_t len, os_model **out);
+os_status os_model_load_file(const char *path, os_model **out);
+void os_model_free(os_model *model);
+
+/* QUBOModel::get_nodes (qubo.hpp:177-180): max used index + 1. */
+int64_t os_model_nodes(const os_model *model);
+/* Number of stored linear / quadratic coefficients. */
+int64_t os_model_num_linear(const os_model *model);
+int64_t os_model_num_quadratic(const os_model *model);
+/* QUBOModel::get_variable / get_connection (qubo.hpp:216-240): a missing
+ * key reads as 0. */
+double os_model_get_variable(const os_model *model, int32_t i);
+double os_model_get_connection(const os_model *model, int32_t i, int32_t j);
+/* helpers::flatten_qubo (qubo_helpers.hpp:26-44) into out[n*n]. */
+os_status os_model_flatten(const os_model *model, double *out, size_t cap);
+/* QUBOModel::str (qubo.hpp:182-202). Writes a NUL-terminated string;
+ * *len_out gets the full length (excluding NUL). */
+os_status os_model_str(const os_model *model, char *out, size_t cap, size_t *len_out);
+
+/* qubo::Solution::save (include/model/solution.hpp:58-67): the two-line CSV
+ * with the energy at 6 significant digits. */
+os_status os_solution_csv(const char *state, int32_t n, double energy,
+                          char *out, size_t cap, size_t *len_out);
+
+/* ------------------------------------------------------------------------ */
+/* Exhaustive search                                                        */
+/* ------------------------------------------------------------------------ */
+
+typedef struct os_qubo_dense {
+  int32_t n;         /* number of variables */
+  const double *f;   /* n*n flattened matrix (host), upper triangle read */
+} os_qubo_dense;
+
+typedef enum os_coef_kind {
+  OS_COEF_AUTO = 0,     /* int32 if every coefficient is an integer and the
+                           energy range fits, else int64, else fixed64 */
+  OS_COEF_INT32 = 1,    /* exact int32 Gray-code enumeration */
+  OS_COEF_INT64 = 2,    /* exact int64 Gray-code enumeration */
+  OS_COEF_FIXED64 = 3   /* non-integer coefficients: int64 fixed-point
+                           enumeration, then a candidate window re-scored in
+                           FP64 in the reference's summation order */
+} os_coef_kind;
+
+typedef struct os_exh_params {
+  int32_t coef_kind;        /* os_coef_kind */
+  int32_t fixed_high_bits;  /* 0 = whole space; k > 0 fixes the top k bits */
+  uint64_t prefix;          /* value of the fixed top bits (shard index) */
+  uint64_t max_minimisers;  /* capacity of os_exh_result.states */
+} os_exh_params;
+
+typedef struct os_exh_result {
+  double energy;              /* ground energy under the reference's FP64
+                                 energy function (exhaustive.hpp:112-129) */
+  uint64_t state;             /* smallest minimising state: the one the
+                                 reference returns (exhaustive.hpp:130-133,158-166) */
+  uint64_t count;             /* total number of degenerate minimisers */
+  uint64_t *states;           /* caller buffer; min(count, max_minimisers)
+                                 minimisers in ascending order (may be NULL
+                                 when max_minimisers is 0) */
+  uint64_t states_enumerated; /* 2^(n - fixed_high_bits) */
+  int32_t coef_kind_used;     /* os_coef_kind actually run */
+  int32_t collect_passes;     /* 1, or 2 when the degenerate set needed a
+                                 second collection pass */
+} os_exh_result;
+
+/* Replaces exhaustive::solve (include/exhaustive/exhaustive.hpp:29-167).
+ * Host buffers in and out; the call uploads the QUBO, enumerates all states
+ * on the GPU, and returns the ground energy, the reference's minimiser and
+ * the full degenerate set. n may be 1..50 (the reference's own limit is 30,
+ * exhaustive.hpp:67 and ulong_to_vec.hpp:24-26). Returns
+ * OS_OVERFLOW_MINIMISERS (with count and the first max_minimisers states
+ * filled in) when the degenerate set is larger than the caller's buffer. */
+os_status os_exhaustive_run(os_ctx *ctx, const os_qubo_dense *qubo,
+                            const os_exh_params *params, os_exh_result *result);
+
+/* The same search split into device-resident steps, for callers that keep
+ * the problem on the GPU across calls (and for timing the kernels alone):
+ * create uploads and prepares the problem, execute only enqueues the
+ * enumeration kernels on the context's stream, result synchronises, runs a
+ * second collection pass if the first overflowed, and copies the answer
+ * back. No reference counterpart (the reference's solve is one call). */
+typedef struct os_exh_plan os_exh_plan;
+os_status os_exhaustive_plan_create(os_ctx *ctx, const os_qubo_dense *qubo,
+                                    const os_exh_params *params,
+                                    os_exh_plan **out);
+os_status os_exhaustive_plan_execute(os_exh_plan *plan);
+os_status os_exhaustive_plan_result(os_exh_plan *plan, os_exh_result *result);
+/* Kernel launches made by the last execute (for launch accounting). */
+int32_t os_exhaustive_plan_launches(const os_exh_plan *plan);
+/* Device time of the last execute's enumeration kernel, from CUDA events
+ * recorded on the context's stream around it (waits for it to finish). */
+os_status os_exhaustive_plan_kernel_ms(os_exh_plan *plan, float *ms);
+void os_exhaustive_plan_destroy(os_exh_plan *plan);
+
+/* ------------------------------------------------------------------------ */
+/* Simulated annealing                                                      */
+/* ------------------------------------------------------------------------ */
+
+typedef enum os_acceptance {
+  OS_ACCEPT_REFERENCE = 0,  /* exp((E_cur - E_new) / beta) > u, as the
+                               reference does (annealing.hpp:106-108) */
+  OS_ACCEPT_PHYSICAL = 1    /* exp(-beta * (E_new - E_cur)) > u */
+} os_acceptance;
+
+typedef enum os_site_order {
+  OS_SITES_RANDOM = 0,      /* one step = one attempt at a uniformly random
+                               site (the reference, annealing.hpp:97-101) */
+  OS_SITES_SEQUENTIAL = 1   /* one step = one sweep: an attempt at every
+                               site in a fixed order (n attempts) */
+} os_site_order;
+
+typedef struct os_sa_params {
+  const double *beta;       /* num_iter values (host); the schedule */
+  int32_t num_iter;         /* schedule length (annealing.hpp:56-57) */
+  int32_t sweeps_per_beta;  /* steps per beta value (annealing.hpp:58) */
+  uint32_t num_tries;       /* independent trajectories (annealing.hpp:57) */
+  uint64_t seed;            /* Philox key; replaces the fixed 1234 of
+                               annealing.hpp:87 */
+  int32_t acceptance;       /* os_acceptance */
+  int32_t site_order;       /* os_site_order */
+  int32_t resync_every;     /* steps between FP64 local-field resyncs
+                               (0 = only one check at the end) */
+  const float *init_prob;   /* optional n values: P(x_i = 1) at start (warm
+                               start); NULL = fair coin per spin as the
+                               reference's bit() (annealing.hpp:91-93) */
+} os_sa_params;
+
+typedef struct os_sa_result {
+  char *state;              /* [n] best state over all trajectories */
+  double energy;            /* its energy, re-scored in FP64 with the
+                               reference's energy function */
+  double *traj_energies;    /* optional [num_tries]: FP64 re-scored best
+                               energy of each trajectory */
+  char *traj_states;        /* optional [num_tries * n] best states */
+  double max_field_drift;   /* max |h_fp32 - h_fp64| over resyncs */
+  uint64_t attempts;        /* spin-flip attempts performed */
+  uint64_t accepted;        /* accepted flips */
+} os_sa_result;
+
+/* Replaces sa::anneal (include/simulated_annealing/annealing.hpp:55-140).
+ * Dense QUBO, host buffers in and out. Trajectories run on the GPU with
+ * FP32 local fields (FP64 resync), counter-based Philox randoms per
+ * (trajectory, step, site), and the host-side argmin of annealing.hpp:134-139
+ * (first minimum of the re-scored energies). */
+os_status os_sa_run(os_ctx *ctx, const os_qubo_dense *qubo,
+                    const os_sa_params *params, os_sa_result *result);
+
+/* Sparse QUBO in CSR form: the off-diagonal couplings of row i are
+ * col[row_ptr[i] .. row_ptr[i+1]) with values val (both triangles present,
+ * i.e. the symmetric flattened matrix without its zeros), diag[i] = linear
+ * term. */
+typedef struct os_qubo_csr {
+  int32_t n;
+  const int32_t *row_ptr;   /* n+1 */
+  const int32_t *col;       /* nnz */
+  const double *val;        /* nnz */
+  const double *diag;       /* n */
+} os_qubo_csr;
+
+/* sa::anneal on a sparse QUBO (e.g. Chimera droplet instances,
+ * benchmarks/annealing/chimera_droplets_qbsolv): sites are coloured so that
+ * no two sites of a colour are coupled, and one sweep updates the colours in
+ * order, every site of a colour in parallel. This is the sequential sweep in
+ * colour-sorted site order. Requires site_order = OS_SITES_SEQUENTIAL. */
+os_status os_sa_run_sparse(os_ctx *ctx, const os_qubo_csr *qubo,
+                           const os_sa_params *params, os_sa_result *result);
+
+/* Deterministic verification mode. Runs the reference's Metropolis rule
+ * (annealing.hpp:87-125) on the GPU with caller-given randoms in place of
+ * oneMKL's philox4x32x10: init[t*n+i] replaces bit(), site[t*S+a] replaces
+ * bit_index() and u[t*S+a] replaces uniform() for attempt a of trajectory t,
+ * S = num_iter * sweeps_per_beta. One (site, u) pair is consumed per attempt
+ * whether or not u is needed. Energies are tracked from FP64 local fields;
+ * for integer-valued coefficients they equal the reference's per-attempt
+ * full recomputation exactly, so the spin trajectories are bit-identical.
+ * Outputs per trajectory: best state and energy, final state and energy,
+ * accepted-flip count (any output pointer may be NULL). */
+os_status os_sa_verify(os_ctx *ctx, const os_qubo_dense *qubo,
+                       const double *beta, int32_t num_iter,
+                       int32_t sweeps_per_beta, uint32_t num_tries,
+                       int32_t acceptance, const char *init,
+                       const int32_t *site, const double *u,
+                       char *best_states, double *best_energies,
+                       char *final_states, double *final_energies,
+                       int64_t *accept_count);
+
+/* FP64 energies of m states under the reference's energy function
+ * (annealing.hpp:31-40), computed on the GPU in the same summation order.
+ * states is m*n chars (host), energies m doubles (host). */
+os_status os_energy_batch(os_ctx *ctx, const os_qubo_dense *qubo,
+                          const char *states, int32_t m, double *energies);
+
+/* Device-resident SA plan (dense or sparse): create uploads the instance and
+ * schedule, execute enqueues one whole anneal (all trajectories, all
+ * steps) on the context's stream, result synchronises and copies the answer
+ * back. No reference counterpart. */
+typedef struct os_sa_plan os_sa_plan;
+os_status os_sa_plan_create_dense(os_ctx *ctx, const os_qubo_dense *qubo,
+                                  const os_sa_params *params, os_sa_plan **out);
+os_status os_sa_plan_create_sparse(os_ctx *ctx, const os_qubo_csr *qubo,
+                                   const os_sa_params *params, os_sa_plan **out);
+os_status os_sa_plan_execute(os_sa_plan *plan);
+os_status os_sa_plan_result(os_sa_plan *plan, os_sa_result *result);
+int32_t os_sa_plan_launches(const os_sa_plan *plan);
+/* Device time of the last execute's sweep kernels (sum over launches), from
+ * CUDA events recorded on the context's stream around each of them. */
+os_status os_sa_plan_kernel_ms(os_sa_plan *plan, float *ms);
+void os_sa_plan_destroy(os_sa_plan *plan);
+
+/* Philox4x32-10 of the device generator, evaluated on the GPU for `count`
+ * consecutive counters starting at ctr (ctr[0] incremented); out receives
+ * 4*count words. For checking the generator against its published
+ * definition. No reference counterpart. */
+os_status os_philox_sample(os_ctx *ctx, const uint32_t ctr[4],
+                           const uint32_t key[2], int32_t count,
+                           uint32_t *out);
+
+/* Measured roofline denominators for the two integer/FP32-bound paths (the
+ * measured peaks cover HBM copy bandwidth and bf16 GEMMs only): the
+ * INT32 issue rate of the enumeration's per-state instruction pair (three-
+ * input add, integer min), in Gop/s, and the FP32 FMA rate, in GFLOP/s.
+ * No reference counterpart. */
+os_status os_probe_int32_peak(os_ctx *ctx, double *gops);
+os_status os_probe_fp32_fma_peak(os_ctx *ctx, double *gflops);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* ONESOLVER_H_ */

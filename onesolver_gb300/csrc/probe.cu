@@ -1,0 +1,140 @@
+// probe.cu -- measured roofline denominators that the driver does not
+// provide: the INT32 issue rate of the exhaustive kernel's per-state
+// instruction pair (three-input add with a constant-bank operand, then an
+// integer min), and the FP32 FMA rate of the annealing field updates.
+#include <cstdint>
+#include <utility>
+
+#include "common.cuh"
+
+namespace os {
+namespace probe {
+
+constexpr int STEPS = 256;
+constexpr int CHAINS = 4;
+
+struct ProbeParams {
+  int k[STEPS];
+  int iters;
+  int *sink;
+};
+
+template <int I>
+__device__ __forceinline__ void step(int (&E)[CHAINS], int (&m)[CHAINS], const int (&c)[CHAINS],
+                                     const ProbeParams &P) {
+#pragma unroll
+  for (int j = 0; j < CHAINS; ++j) {
+    E[j] += P.k[I] + ((I & 1) ? c[j] : -c[j]);
+    m[j] = min(m[j], E[j]);
+  }
+}
+
+template <int... Is>
+__device__ __forceinline__ void steps(int (&E)[CHAINS], int (&m)[CHAINS], const int (&c)[CHAINS],
+                                      const ProbeParams &P, std::integer_sequence<int, Is...>) {
+  (step<Is>(E, m, c, P), ...);
+}
+
+// Per iteration: STEPS * CHAINS (add, min) pairs = 2 * STEPS * CHAINS ops.
+__global__ void __launch_bounds__(256) int32_probe_kernel(const __grid_constant__ ProbeParams P) {
+  int E[CHAINS], m[CHAINS], c[CHAINS];
+#pragma unroll
+  for (int j = 0; j < CHAINS; ++j) {
+    E[j] = threadIdx.x * 7 + j;
+    m[j] = 1 << 30;
+    c[j] = (blockIdx.x + j) & 3;
+  }
+  for (int it = 0; it < P.iters; ++it) {
+    steps(E, m, c, P, std::make_integer_sequence<int, STEPS>{});
+#pragma unroll
+    for (int j = 0; j < CHAINS; ++j) c[j] ^= m[j] & 1;
+  }
+  int r = 0;
+#pragma unroll
+  for (int j = 0; j < CHAINS; ++j) r ^= m[j] ^ E[j];
+  if (r == 0x7fffffff) P.sink[0] = r;
+}
+
+// Per iteration: 8 independent FMA chains x 64 steps.
+__global__ void __launch_bounds__(256) fp32_probe_kernel(int iters, float a, float b, float *sink) {
+  float v[8];
+#pragma unroll
+  for (int j = 0; j < 8; ++j) v[j] = threadIdx.x * 1e-3f + j;
+  for (int it = 0; it < iters; ++it) {
+#pragma unroll
+    for (int s = 0; s < 64; ++s)
+#pragma unroll
+      for (int j = 0; j < 8; ++j) v[j] = fmaf(v[j], a, b);
+  }
+  float r = 0.f;
+#pragma unroll
+  for (int j = 0; j < 8; ++j) r += v[j];
+  if (r == 1234.5f) sink[0] = r;
+}
+
+template <class F> double time_ms(cudaStream_t s, F &&launch) {
+  cudaEvent_t e0, e1;
+  OS_CUDA(cudaEventCreate(&e0));
+  OS_CUDA(cudaEventCreate(&e1));
+  launch();  // warm-up
+  OS_CUDA(cudaEventRecord(e0, s));
+  launch();
+  OS_CUDA(cudaEventRecord(e1, s));
+  OS_CUDA(cudaEventSynchronize(e1));
+  float ms = 0.f;
+  OS_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  return ms;
+}
+
+}  // namespace probe
+}  // namespace os
+
+using namespace os;
+using namespace os::probe;
+
+extern "C" {
+
+os_status os_probe_int32_peak(os_ctx *ctx, double *gops) {
+  return guard([&] {
+    activate(ctx);
+    OS_REQUIRE(gops != nullptr, "null output");
+    DevBuf<int> sink;
+    sink.alloc(1);
+    ProbeParams P{};
+    for (int i = 0; i < STEPS; ++i) P.k[i] = (i * 2654435761u) & 15;
+    P.iters = 64;
+    P.sink = sink.get();
+    int occ = 0;
+    OS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, int32_probe_kernel, 256, 0));
+    const int grid = ctx->sm_count * (occ > 0 ? occ : 1);
+    const double ms = time_ms(ctx->stream, [&] {
+      int32_probe_kernel<<<grid, 256, 0, ctx->stream>>>(P);
+      OS_CUDA(cudaGetLastError());
+    });
+    const double ops = 2.0 * STEPS * CHAINS * (double)P.iters * grid * 256.0;
+    *gops = ops / (ms * 1e-3) / 1e9;
+  });
+}
+
+os_status os_probe_fp32_fma_peak(os_ctx *ctx, double *gflops) {
+  return guard([&] {
+    activate(ctx);
+    OS_REQUIRE(gflops != nullptr, "null output");
+    DevBuf<float> sink;
+    sink.alloc(1);
+    int occ = 0;
+    OS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fp32_probe_kernel, 256, 0));
+    const int grid = ctx->sm_count * (occ > 0 ? occ : 1);
+    const int iters = 512;
+    const double ms = time_ms(ctx->stream, [&] {
+      fp32_probe_kernel<<<grid, 256, 0, ctx->stream>>>(iters, 0.999f, 0.001f, sink.get());
+      OS_CUDA(cudaGetLastError());
+    });
+    const double flops = 2.0 * 64 * 8 * (double)iters * grid * 256.0;
+    *gflops = flops / (ms * 1e-3) / 1e9;
+  });
+}
+
+}  // extern "C"

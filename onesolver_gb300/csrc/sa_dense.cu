@@ -1,0 +1,422 @@
+// sa_dense.cu -- dense simulated annealing: the verification kernel, the
+// device-resident plan and the os_sa_run / os_sa_verify entry points.
+//
+// Replaces sa::anneal (include/simulated_annealing/annealing.hpp:55-140).
+// One anneal is: draw the initial spins and compute the FP64 fields; run the
+// schedule in chunks of resync_every steps, with an FP64 field resync (and
+// drift measurement) between chunks; re-score every trajectory's best state
+// with the reference's FP64 energy function; take the first minimum on the
+// host (annealing.hpp:134-139).
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "common.cuh"
+#include "rescore.cuh"
+#include "sa_common.cuh"
+#include "sa_kernels.cuh"
+#include "sa_plan.cuh"
+
+namespace os {
+namespace sa {
+
+// Deterministic verification: one thread per trajectory replays the
+// reference's kernel body (annealing.hpp:87-125) with caller-given randoms.
+// Fields are FP64 and the energy is the reference's initial FP64 energy plus
+// the FP64 deltas, which equals the reference's per-attempt recomputation
+// exactly whenever the coefficients are integers.
+__global__ void sa_verify_kernel(const double *__restrict__ f, int n, const double *__restrict__ beta,
+                                 int num_iter, int spb, int T, int acceptance,
+                                 const uint8_t *__restrict__ init, const int *__restrict__ site,
+                                 const double *__restrict__ u, double *__restrict__ hbuf,
+                                 uint8_t *__restrict__ cur, uint8_t *__restrict__ best,
+                                 double *__restrict__ ebest, double *__restrict__ efinal,
+                                 long long *__restrict__ acc_out) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= T) return;
+  const long long S = (long long)num_iter * spb;
+  uint8_t *x = cur + (size_t)t * n;
+  uint8_t *bx = best + (size_t)t * n;
+  double *h = hbuf + (size_t)t * n;
+  for (int i = 0; i < n; ++i) x[i] = bx[i] = init[(size_t)t * n + i] ? 1 : 0;
+  // Fields from the symmetric couplings (f holds the upper triangle).
+  for (int j = 0; j < n; ++j) {
+    double acc = 0.0;
+    for (int i = 0; i < n; ++i) {
+      if (i == j || !x[i]) continue;
+      acc += i < j ? f[(size_t)i * n + j] : f[(size_t)j * n + i];
+    }
+    h[j] = acc;
+  }
+  double E = rescore_energy(f, n, x);
+  double Eb = E;
+  long long accepted = 0;
+  for (int it = 0; it < num_iter; ++it) {
+    const double b = beta[it];
+    for (int sw = 0; sw < spb; ++sw) {
+      const long long a = (long long)it * spb + sw;
+      const int k = site[(size_t)t * S + a];
+      const double uu = u[(size_t)t * S + a];
+      const double loc = f[(size_t)k * n + k] + h[k];
+      const double dE = x[k] ? -loc : loc;
+      const double Enew = E + dE;
+      bool accept;
+      if (Enew < E)
+        accept = true;
+      else if (acceptance == OS_ACCEPT_REFERENCE)
+        accept = exp((E - Enew) / b) > uu;
+      else
+        accept = exp(-b * (Enew - E)) > uu;
+      if (accept) {
+        x[k] ^= 1;
+        const double sgn = x[k] ? 1.0 : -1.0;
+        for (int j = 0; j < n; ++j) {
+          if (j == k) continue;
+          h[j] += sgn * (j < k ? f[(size_t)j * n + k] : f[(size_t)k * n + j]);
+        }
+        E = Enew;
+        ++accepted;
+      }
+      if (E < Eb) {
+        Eb = E;
+        for (int i = 0; i < n; ++i) bx[i] = x[i];
+      }
+    }
+  }
+  ebest[t] = Eb;
+  efinal[t] = E;
+  acc_out[t] = accepted;
+}
+
+template <int SLOTS> void launch_seq(const DenseArgs &a, int warps, cudaStream_t s) {
+  const int grid = (a.traj_count + warps - 1) / warps;
+  sa_dense_seq_kernel<SLOTS><<<grid, warps * 32, 0, s>>>(a);
+}
+template <int SLOTS> void launch_rand(const DenseArgs &a, int warps, cudaStream_t s) {
+  const int grid = (a.traj_count + warps - 1) / warps;
+  sa_dense_rand_kernel<SLOTS><<<grid, warps * 32, 0, s>>>(a);
+}
+template <int SLOTS> void launch_resync(const ResyncArgs &a, int warps, cudaStream_t s) {
+  const int grid = (a.traj_count + warps - 1) / warps;
+  sa_dense_resync_kernel<SLOTS><<<grid, warps * 32, 0, s>>>(a);
+}
+
+#define OS_SLOT_DISPATCH(cls, fn, ...)                                  \
+  switch (cls) {                                                        \
+    case 1: fn<1>(__VA_ARGS__); break;                                  \
+    case 2: fn<2>(__VA_ARGS__); break;                                  \
+    case 4: fn<4>(__VA_ARGS__); break;                                  \
+    case 8: fn<8>(__VA_ARGS__); break;                                  \
+    case 16: fn<16>(__VA_ARGS__); break;                                \
+    case 32: fn<32>(__VA_ARGS__); break;                                \
+    case 64: fn<64>(__VA_ARGS__); break;                                \
+    default: throw_error(OS_INVALID_ARG, "unsupported slot count %d", cls); \
+  }
+
+void dense_sweeps(const DenseArgs &a, int slot_cls, int warps, bool sequential, cudaStream_t s) {
+  if (sequential) {
+    OS_SLOT_DISPATCH(slot_cls, launch_seq, a, warps, s);
+  } else {
+    OS_SLOT_DISPATCH(slot_cls, launch_rand, a, warps, s);
+  }
+  OS_CUDA(cudaGetLastError());
+}
+
+void dense_resync(const ResyncArgs &a, int slot_cls, int warps, cudaStream_t s) {
+  OS_SLOT_DISPATCH(slot_cls, launch_resync, a, warps, s);
+  OS_CUDA(cudaGetLastError());
+}
+
+// Warps per CTA: spread small trajectory counts over all SMs.
+int dense_warps(int traj, int sm_count) {
+  if (traj <= sm_count * 4) return 1;
+  if (traj <= sm_count * 16) return 2;
+  return 4;
+}
+
+void plan_create_dense(os_sa_plan *p, const os_qubo_dense *q) {
+  OS_REQUIRE(q && q->f, "null QUBO");
+  OS_REQUIRE(q->n >= 1 && q->n <= MAX_DENSE_N, "dense annealing supports 1..%d variables (got %d)",
+             MAX_DENSE_N, q->n);
+  DenseHost hst;
+  stage_dense(q, hst);
+  p->n = hst.n;
+  p->nslots = hst.nslots;
+  p->ld = hst.ld;
+  p->slot_cls = slot_class(hst.nslots);
+  const size_t T = p->T;
+  p->c32.alloc(hst.c32.size());
+  p->d32.alloc(hst.d32.size());
+  p->c64.alloc(hst.c64.size());
+  p->d64.alloc(hst.d64.size());
+  p->f.alloc(hst.f.size());
+  OS_CUDA(cudaMemcpy(p->c32.get(), hst.c32.data(), sizeof(float) * hst.c32.size(), cudaMemcpyHostToDevice));
+  OS_CUDA(cudaMemcpy(p->d32.get(), hst.d32.data(), sizeof(float) * hst.d32.size(), cudaMemcpyHostToDevice));
+  OS_CUDA(cudaMemcpy(p->c64.get(), hst.c64.data(), sizeof(double) * hst.c64.size(), cudaMemcpyHostToDevice));
+  OS_CUDA(cudaMemcpy(p->d64.get(), hst.d64.data(), sizeof(double) * hst.d64.size(), cudaMemcpyHostToDevice));
+  OS_CUDA(cudaMemcpy(p->f.get(), hst.f.data(), sizeof(double) * hst.f.size(), cudaMemcpyHostToDevice));
+  p->h.alloc(T * hst.nslots * 32);
+  p->x.alloc(T * 32);
+  p->xbest.alloc(T * 32);
+  p->e.alloc(T);
+  p->ebest.alloc(T);
+  p->accepted.alloc(T);
+  p->states.alloc(T * (size_t)hst.n);
+  p->e64.alloc(T);
+  p->warps = dense_warps((int)T, p->ctx->sm_count);
+}
+
+void execute_dense(os_sa_plan *p) {
+  cudaStream_t s = p->ctx->stream;
+  p->launches = 0;
+  OS_CUDA(cudaMemsetAsync(p->accepted.get(), 0, sizeof(unsigned long long) * p->T, s));
+  OS_CUDA(cudaMemsetAsync(p->drift.get(), 0, sizeof(unsigned long long), s));
+  ResyncArgs r{};
+  r.c64 = p->c64.get();
+  r.d64 = p->d64.get();
+  r.n = p->n;
+  r.nslots = p->nslots;
+  r.ld = p->ld;
+  r.init = 1;
+  r.init_prob = p->init_prob.count ? p->init_prob.get() : nullptr;
+  r.traj_count = p->T;
+  r.traj_offset = 0;
+  r.seed_lo = (uint32_t)p->seed;
+  r.seed_hi = (uint32_t)(p->seed >> 32);
+  r.instance = 0;
+  r.h = p->h.get();
+  r.x = p->x.get();
+  r.xbest = p->xbest.get();
+  r.e = p->e.get();
+  r.ebest = p->ebest.get();
+  r.drift_bits = p->drift.get();
+  dense_resync(r, p->slot_cls, p->warps, s);
+  ++p->launches;
+
+  DenseArgs a{};
+  a.c = p->c32.get();
+  a.diag = p->d32.get();
+  a.n = p->n;
+  a.nslots = p->nslots;
+  a.ld = p->ld;
+  a.spb = p->spb;
+  a.beta = p->beta.get();
+  a.acceptance = p->acceptance;
+  a.traj_count = p->T;
+  a.traj_offset = 0;
+  a.seed_lo = r.seed_lo;
+  a.seed_hi = r.seed_hi;
+  a.instance = 0;
+  a.h = p->h.get();
+  a.x = p->x.get();
+  a.xbest = p->xbest.get();
+  a.e = p->e.get();
+  a.ebest = p->ebest.get();
+  a.accepted = p->accepted.get();
+  r.init = 0;
+  const int chunk = p->chunk;
+  p->sweep_ev_used = 0;
+  for (int s0 = 0; s0 < p->steps; s0 += chunk) {
+    a.step_begin = s0;
+    a.step_end = std::min(p->steps, s0 + chunk);
+    OS_CUDA(cudaEventRecord(p->event(2 * p->sweep_ev_used), s));
+    dense_sweeps(a, p->slot_cls, p->warps, p->sequential, s);
+    OS_CUDA(cudaEventRecord(p->event(2 * p->sweep_ev_used + 1), s));
+    ++p->sweep_ev_used;
+    dense_resync(r, p->slot_cls, p->warps, s);
+    p->launches += 2;
+  }
+  const size_t total = (size_t)p->T * p->n;
+  unpack_states_kernel<<<(unsigned)ceil_div_u64(total, 256), 256, 0, s>>>(p->xbest.get(), p->n, p->T,
+                                                                        p->states.get());
+  OS_CUDA(cudaGetLastError());
+  launch_rescore(p->f.get(), p->n, p->states.get(), p->T, p->e64.get(), s);
+  p->launches += 2;
+}
+
+}  // namespace sa
+}  // namespace os
+
+using namespace os;
+using namespace os::sa;
+
+// Common plan set-up: schedule, seeds, chunking.
+void os_sa_plan_common(os_sa_plan *p, os_ctx *ctx, const os_sa_params *prm, int n) {
+  p->ctx = ctx;
+  p->T = (int)prm->num_tries;
+  p->spb = prm->sweeps_per_beta;
+  p->num_iter = prm->num_iter;
+  const long long steps = (long long)prm->num_iter * prm->sweeps_per_beta;
+  OS_REQUIRE(steps < (1ll << 31), "too many steps (%lld)", steps);
+  p->steps = (int)steps;
+  p->chunk = prm->resync_every > 0 ? prm->resync_every : p->steps;
+  p->seed = prm->seed;
+  p->acceptance = prm->acceptance;
+  p->sequential = prm->site_order == OS_SITES_SEQUENTIAL;
+  p->attempts_per_step = p->sequential ? (unsigned long long)n : 1ull;
+  p->beta.alloc(prm->num_iter);
+  OS_CUDA(cudaMemcpy(p->beta.get(), prm->beta, sizeof(double) * prm->num_iter, cudaMemcpyHostToDevice));
+  if (prm->init_prob) {
+    for (int i = 0; i < n; ++i)
+      OS_REQUIRE(prm->init_prob[i] >= 0.f && prm->init_prob[i] <= 1.f, "init_prob[%d] outside [0,1]", i);
+    p->init_prob.alloc(n);
+    OS_CUDA(cudaMemcpy(p->init_prob.get(), prm->init_prob, sizeof(float) * n, cudaMemcpyHostToDevice));
+  }
+  p->drift.alloc(1);
+}
+
+os_status os_sa_plan_result(os_sa_plan *p, os_sa_result *res) {
+  return guard([&] {
+    OS_REQUIRE(p && res, "null argument");
+    activate(p->ctx);
+    cudaStream_t s = p->ctx->stream;
+    OS_CUDA(cudaStreamSynchronize(s));
+    const int T = p->T, n = p->n;
+    std::vector<double> e(T);
+    OS_CUDA(cudaMemcpy(e.data(), p->e64.get(), sizeof(double) * T, cudaMemcpyDeviceToHost));
+    std::vector<unsigned long long> acc(T);
+    OS_CUDA(cudaMemcpy(acc.data(), p->accepted.get(), sizeof(unsigned long long) * T, cudaMemcpyDeviceToHost));
+    unsigned long long drift_bits = 0;
+    OS_CUDA(cudaMemcpy(&drift_bits, p->drift.get(), sizeof drift_bits, cudaMemcpyDeviceToHost));
+    const int best = argmin_first(e);
+    if (res->state)
+      OS_CUDA(cudaMemcpy(res->state, p->states.get() + (size_t)best * n, n, cudaMemcpyDeviceToHost));
+    if (res->traj_states)
+      OS_CUDA(cudaMemcpy(res->traj_states, p->states.get(), (size_t)T * n, cudaMemcpyDeviceToHost));
+    if (res->traj_energies) std::memcpy(res->traj_energies, e.data(), sizeof(double) * T);
+    res->energy = e[best];
+    double drift;
+    std::memcpy(&drift, &drift_bits, sizeof drift);
+    res->max_field_drift = drift;
+    res->attempts = (unsigned long long)p->steps * p->attempts_per_step * (unsigned long long)T;
+    unsigned long long total = 0;
+    for (auto v : acc) total += v;
+    res->accepted = total;
+  });
+}
+
+extern "C" {
+
+os_status os_sa_plan_create_dense(os_ctx *ctx, const os_qubo_dense *qubo, const os_sa_params *params,
+                                  os_sa_plan **out) {
+  return guard([&] {
+    activate(ctx);
+    OS_REQUIRE(out != nullptr, "null output");
+    check_schedule(params);
+    OS_REQUIRE(qubo != nullptr, "null QUBO");
+    auto *p = new os_sa_plan();
+    try {
+      p->kind = 0;
+      os_sa_plan_common(p, ctx, params, qubo->n);
+      plan_create_dense(p, qubo);
+    } catch (...) {
+      delete p;
+      throw;
+    }
+    *out = p;
+  });
+}
+
+os_status os_sa_plan_execute(os_sa_plan *p) {
+  return guard([&] {
+    OS_REQUIRE(p != nullptr, "null plan");
+    activate(p->ctx);
+    if (p->kind == 0)
+      execute_dense(p);
+    else
+      execute_sparse(p);
+  });
+}
+
+int32_t os_sa_plan_launches(const os_sa_plan *p) { return p ? p->launches : 0; }
+
+os_status os_sa_plan_kernel_ms(os_sa_plan *p, float *ms) {
+  return guard([&] {
+    OS_REQUIRE(p && ms, "null argument");
+    activate(p->ctx);
+    float total = 0.f;
+    for (int i = 0; i < p->sweep_ev_used; ++i) {
+      float t = 0.f;
+      OS_CUDA(cudaEventSynchronize(p->sweep_ev[2 * i + 1]));
+      OS_CUDA(cudaEventElapsedTime(&t, p->sweep_ev[2 * i], p->sweep_ev[2 * i + 1]));
+      total += t;
+    }
+    *ms = total;
+  });
+}
+
+void os_sa_plan_destroy(os_sa_plan *p) {
+  if (!p) return;
+  cudaSetDevice(p->ctx->device);
+  cudaStreamSynchronize(p->ctx->stream);
+  delete p;
+}
+
+os_status os_sa_run(os_ctx *ctx, const os_qubo_dense *qubo, const os_sa_params *params,
+                    os_sa_result *result) {
+  os_sa_plan *plan = nullptr;
+  os_status st = os_sa_plan_create_dense(ctx, qubo, params, &plan);
+  if (st != OS_OK) return st;
+  st = os_sa_plan_execute(plan);
+  if (st == OS_OK) st = os_sa_plan_result(plan, result);
+  os_sa_plan_destroy(plan);
+  return st;
+}
+
+os_status os_sa_verify(os_ctx *ctx, const os_qubo_dense *qubo, const double *beta, int32_t num_iter,
+                       int32_t sweeps_per_beta, uint32_t num_tries, int32_t acceptance,
+                       const char *init, const int32_t *site, const double *u, char *best_states,
+                       double *best_energies, char *final_states, double *final_energies,
+                       int64_t *accept_count) {
+  return guard([&] {
+    activate(ctx);
+    OS_REQUIRE(qubo && qubo->f && qubo->n >= 1, "bad QUBO");
+    OS_REQUIRE(beta && num_iter > 0 && sweeps_per_beta > 0 && num_tries > 0, "bad schedule");
+    OS_REQUIRE(init && site && u, "null random arrays");
+    OS_REQUIRE(acceptance == OS_ACCEPT_REFERENCE || acceptance == OS_ACCEPT_PHYSICAL,
+               "unknown acceptance rule %d", acceptance);
+    const int n = qubo->n, T = (int)num_tries;
+    const size_t S = (size_t)num_iter * sweeps_per_beta;
+    for (size_t i = 0; i < S * T; ++i)
+      OS_REQUIRE(site[i] >= 0 && site[i] < n, "site[%zu] = %d outside [0, n)", i, site[i]);
+    cudaStream_t s = ctx->stream;
+    DevBuf<double> d_f, d_beta, d_u, d_h, d_eb, d_ef;
+    DevBuf<int> d_site;
+    DevBuf<uint8_t> d_init, d_cur, d_best;
+    DevBuf<long long> d_acc;
+    d_f.alloc((size_t)n * n);
+    d_beta.alloc(num_iter);
+    d_u.alloc(S * T);
+    d_site.alloc(S * T);
+    d_h.alloc((size_t)T * n);
+    d_init.alloc((size_t)T * n);
+    d_cur.alloc((size_t)T * n);
+    d_best.alloc((size_t)T * n);
+    d_eb.alloc(T);
+    d_ef.alloc(T);
+    d_acc.alloc(T);
+    OS_CUDA(cudaMemcpyAsync(d_f.get(), qubo->f, sizeof(double) * n * n, cudaMemcpyHostToDevice, s));
+    OS_CUDA(cudaMemcpyAsync(d_beta.get(), beta, sizeof(double) * num_iter, cudaMemcpyHostToDevice, s));
+    OS_CUDA(cudaMemcpyAsync(d_u.get(), u, sizeof(double) * S * T, cudaMemcpyHostToDevice, s));
+    OS_CUDA(cudaMemcpyAsync(d_site.get(), site, sizeof(int) * S * T, cudaMemcpyHostToDevice, s));
+    OS_CUDA(cudaMemcpyAsync(d_init.get(), init, (size_t)T * n, cudaMemcpyHostToDevice, s));
+    sa_verify_kernel<<<(T + 63) / 64, 64, 0, s>>>(d_f.get(), n, d_beta.get(), num_iter, sweeps_per_beta, T,
+                                                  acceptance, d_init.get(), d_site.get(), d_u.get(), d_h.get(),
+                                                  d_cur.get(), d_best.get(), d_eb.get(), d_ef.get(), d_acc.get());
+    OS_CUDA(cudaGetLastError());
+    if (best_states)
+      OS_CUDA(cudaMemcpyAsync(best_states, d_best.get(), (size_t)T * n, cudaMemcpyDeviceToHost, s));
+    if (final_states)
+      OS_CUDA(cudaMemcpyAsync(final_states, d_cur.get(), (size_t)T * n, cudaMemcpyDeviceToHost, s));
+    if (best_energies)
+      OS_CUDA(cudaMemcpyAsync(best_energies, d_eb.get(), sizeof(double) * T, cudaMemcpyDeviceToHost, s));
+    if (final_energies)
+      OS_CUDA(cudaMemcpyAsync(final_energies, d_ef.get(), sizeof(double) * T, cudaMemcpyDeviceToHost, s));
+    if (accept_count)
+      OS_CUDA(cudaMemcpyAsync(accept_count, d_acc.get(), sizeof(long long) * T, cudaMemcpyDeviceToHost, s));
+    OS_CUDA(cudaStreamSynchronize(s));
+  });
+}
+
+}  // extern "C"

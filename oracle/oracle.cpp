@@ -1,0 +1,427 @@
+// oracle.cpp -- CPU restatement of oneSolver's two hot paths.
+//
+// TEST INFRASTRUCTURE ONLY. This file is the checker: the pytest suite, the
+// smoke check and the CPU-baseline leg of bench.py load it (through
+// liboracle.so) to verify the GPU library and to time the reference's
+// algorithm on host cores. The product (libonesolver.so) never links or
+// calls it.
+//
+// Every function restates the reference algorithm it cites (paths are
+// relative to the quantumz-io/oneSolver project root). The reference itself
+// cannot be compiled here (it needs a SYCL compiler, Boost and oneMKL), so
+// parity is pinned by checking this restatement against the reference's own
+// known-answer tests (tests/exhaustive_test.cpp, tests/qubo_helpers_test.cpp).
+//
+// Conventions shared with the GPU library:
+//   * a QUBO of n variables is staged as the reference's flat matrix
+//     F (n*n doubles, row-major, symmetric, diagonal = linear terms),
+//     produced by orc_flatten (helpers::flatten_qubo);
+//   * a state is n chars, one 0/1 value per variable, variable 0 first;
+//     exhaustive-search states are uint64 with bit i = variable i
+//     (helpers::ulong_to_vec, include/helpers/ulong_to_vec.hpp:23-32).
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <limits>
+#include <string>
+#include <thread>
+#include <vector>
+
+namespace {
+
+// sa::energy, include/simulated_annealing/annealing.hpp:31-40.
+// E(x) = sum_{i<=j} F[i*n+j] * x_i * x_j, accumulated in FP64 in row-major
+// order over the upper triangle. Multiplying by 0/1 chars is exact, so the
+// value equals the ordered sum of F[i][j] over the pairs with both bits set.
+double energy_ref(const double *flat, const char *state, int n) {
+  double result = 0.0;
+  for (int i = 0; i < n; i++) {
+    for (int j = i; j < n; j++) {
+      result += flat[(size_t)i * n + j] * state[i] * state[j];
+    }
+  }
+  return result;
+}
+
+// Inner loop of exhaustive::solve, include/exhaustive/exhaustive.hpp:112-129:
+// the same ordered FP64 sum, written over the bits of a state integer.
+double energy_state_bits(const double *flat, int n, uint64_t state) {
+  double e = 0.0;
+  for (int i = 0; i < n; ++i) {
+    for (int j = i; j < n; ++j) {
+      if (i == j) {
+        if ((state >> i) & 1ull) e += flat[(size_t)i * n + i];
+      } else {
+        if (((state >> i) & 1ull) && ((state >> j) & 1ull))
+          e += flat[(size_t)i * n + j];
+      }
+    }
+  }
+  return e;
+}
+
+// Philox4x32-10 (Salmon, Moraes, Dror, Shaw, "Parallel random numbers: as
+// easy as 1, 2, 3", SC'11). Restated from the published round function; the
+// GPU library carries its own implementation and the tests compare the two.
+inline void mulhilo32(uint32_t a, uint32_t b, uint32_t &hi, uint32_t &lo) {
+  uint64_t p = (uint64_t)a * (uint64_t)b;
+  hi = (uint32_t)(p >> 32);
+  lo = (uint32_t)p;
+}
+
+void philox4x32_10(const uint32_t ctr_in[4], const uint32_t key_in[2],
+                   uint32_t out[4]) {
+  const uint32_t M0 = 0xD2511F53u, M1 = 0xCD9E8D57u;
+  const uint32_t W0 = 0x9E3779B9u, W1 = 0xBB67AE85u;
+  uint32_t c0 = ctr_in[0], c1 = ctr_in[1], c2 = ctr_in[2], c3 = ctr_in[3];
+  uint32_t k0 = key_in[0], k1 = key_in[1];
+  for (int r = 0; r < 10; ++r) {
+    uint32_t hi0, lo0, hi1, lo1;
+    mulhilo32(M0, c0, hi0, lo0);
+    mulhilo32(M1, c2, hi1, lo1);
+    uint32_t n0 = hi1 ^ c1 ^ k0;
+    uint32_t n1 = lo1;
+    uint32_t n2 = hi0 ^ c3 ^ k1;
+    uint32_t n3 = lo0;
+    c0 = n0; c1 = n1; c2 = n2; c3 = n3;
+    k0 += W0; k1 += W1;
+  }
+  out[0] = c0; out[1] = c1; out[2] = c2; out[3] = c3;
+}
+
+// Small host RNG for the free-running oracle anneal (splitmix64 seeding a
+// xoshiro256** stream, both published generators by Vigna). The oracle's
+// free-running stream is independent of the GPU's Philox stream: the two are
+// compared statistically, never draw by draw.
+struct HostRng {
+  uint64_t s[4];
+  static uint64_t splitmix(uint64_t &x) {
+    uint64_t z = (x += 0x9E3779B97F4A7C15ull);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+  }
+  explicit HostRng(uint64_t seed) {
+    for (int i = 0; i < 4; ++i) s[i] = splitmix(seed);
+  }
+  static uint64_t rotl(uint64_t x, int k) { return (x << k) | (x >> (64 - k)); }
+  uint64_t next() {
+    uint64_t r = rotl(s[1] * 5, 7) * 9;
+    uint64_t t = s[1] << 17;
+    s[2] ^= s[0]; s[3] ^= s[1]; s[1] ^= s[2]; s[0] ^= s[3];
+    s[2] ^= t; s[3] = rotl(s[3], 45);
+    return r;
+  }
+  double uniform() { return (double)(next() >> 11) * 0x1.0p-53; }
+  int below(int n) { return (int)(((next() >> 32) * (uint64_t)n) >> 32); }
+};
+
+}  // namespace
+
+extern "C" {
+
+// helpers::flatten_qubo, include/helpers/qubo_helpers.hpp:26-44.
+// Inputs are the model's coefficient maps as parallel arrays (linear
+// i -> v; quadratic (i,j) -> v with i<j, as QUBOBuilder::add_element stores
+// them, include/model/qubo.hpp:304-318). A key missing from a map reads as 0
+// (QUBOModel::get_variable / get_connection, qubo.hpp:216-240), and
+// get_connection(i,j) with i>j finds no key, so only i<j pairs contribute.
+void orc_flatten(int n, int nlin, const int *lin_i, const double *lin_v,
+                 int nquad, const int *quad_i, const int *quad_j,
+                 const double *quad_v, double *out) {
+  std::vector<double> lin(n, 0.0);
+  for (int k = 0; k < nlin; ++k)
+    if (lin_i[k] >= 0 && lin_i[k] < n) lin[lin_i[k]] = lin_v[k];
+  std::vector<double> quad((size_t)n * n, 0.0);
+  std::vector<char> present((size_t)n * n, 0);
+  for (int k = 0; k < nquad; ++k) {
+    int i = quad_i[k], j = quad_j[k];
+    if (i >= 0 && j >= 0 && i < n && j < n) {
+      quad[(size_t)i * n + j] = quad_v[k];
+      present[(size_t)i * n + j] = 1;
+    }
+  }
+  std::fill(out, out + (size_t)n * n, 0.0);
+  for (int i = 0; i < n; i++) {
+    for (int j = 0; j < n; j++) {
+      if (i == j) {
+        out[(size_t)i + (size_t)j * n] = lin[i];
+      } else {
+        double c = (i < j && present[(size_t)i * n + j]) ? quad[(size_t)i * n + j] : 0.0;
+        out[(size_t)i + (size_t)j * n] += c;
+        out[(size_t)j + (size_t)i * n] += c;
+      }
+    }
+  }
+}
+
+double orc_energy(const double *flat, const char *state, int n) {
+  return energy_ref(flat, state, n);
+}
+
+// Batch re-score: energies of m states (m x n chars).
+void orc_energy_batch(const double *flat, const char *states, int n, int m,
+                      double *out) {
+  for (int t = 0; t < m; ++t) out[t] = energy_ref(flat, states + (size_t)t * n, n);
+}
+
+double orc_energy_bits(const double *flat, int n, uint64_t state) {
+  return energy_state_bits(flat, n, state);
+}
+
+// Beta schedules of app/one-solver-anneal.cpp:23-39, reproduced exactly:
+// linear beta_i = beta_min + beta_max * i / (n-1) (ends at beta_min+beta_max),
+// geometric as a running FP64 product with alpha = (max/min)^(1/(n-1)).
+void orc_schedule_linear(double *out, double beta_min, double beta_max,
+                         unsigned num_iter) {
+  for (unsigned i = 0; i < num_iter; i++)
+    out[i] = beta_min + beta_max * i / static_cast<double>(num_iter - 1);
+}
+
+void orc_schedule_geometric(double *out, double beta_min, double beta_max,
+                            unsigned num_iter) {
+  out[0] = beta_min;
+  double alpha = std::pow(beta_max / beta_min, 1.0 / (num_iter - 1));
+  for (unsigned i = 1; i < num_iter; i++) out[i] = out[i - 1] * alpha;
+}
+
+// Exhaustive search over the state range [begin, end) exactly as the
+// reference's work-item loop (exhaustive.hpp:106-134): FP64 energy per state,
+// keep the first strict minimum. Ranges are split over nthreads host threads
+// the way the reference splits over compute units (exhaustive.hpp:63-90, with
+// the 64-bit shift repaired), and the per-range results are reduced with the
+// first-minimum rule of std::min_element (exhaustive.hpp:158-159). The tie
+// rule therefore returns the smallest state integer among exact minima.
+void orc_exhaustive(const double *flat, int n, uint64_t begin, uint64_t end,
+                    int nthreads, double *e_out, uint64_t *state_out) {
+  if (nthreads < 1) nthreads = 1;
+  uint64_t total = end - begin;
+  std::vector<double> e_best(nthreads, std::numeric_limits<double>::max());
+  std::vector<uint64_t> s_best(nthreads, 0);
+  uint64_t per = total / nthreads, rem = total % nthreads;
+  std::vector<std::thread> pool;
+  uint64_t cursor = begin;
+  for (int t = 0; t < nthreads; ++t) {
+    uint64_t lo = cursor;
+    cursor += per + ((uint64_t)t < rem ? 1 : 0);
+    uint64_t hi = cursor;
+    pool.emplace_back([&, t, lo, hi]() {
+      double eb = std::numeric_limits<double>::max();
+      uint64_t sb = 0;
+      for (uint64_t s = lo; s < hi; ++s) {
+        double e = energy_state_bits(flat, n, s);
+        if (e < eb) { eb = e; sb = s; }
+      }
+      e_best[t] = eb;
+      s_best[t] = sb;
+    });
+  }
+  for (auto &th : pool) th.join();
+  int best = (int)(std::min_element(e_best.begin(), e_best.end()) - e_best.begin());
+  *e_out = e_best[best];
+  *state_out = s_best[best];
+}
+
+// All exact minimisers over [begin, end) under the reference's FP64 energy
+// function: the degenerate ground-state set that the reference's strict-min
+// scan would pick from. Writes up to cap states in ascending order and returns
+// the total count.
+uint64_t orc_exhaustive_all(const double *flat, int n, uint64_t begin,
+                            uint64_t end, int nthreads, double *e_out,
+                            uint64_t *states, uint64_t cap) {
+  if (nthreads < 1) nthreads = 1;
+  double emin;
+  uint64_t smin;
+  orc_exhaustive(flat, n, begin, end, nthreads, &emin, &smin);
+  uint64_t total = end - begin;
+  std::vector<std::vector<uint64_t>> found(nthreads);
+  uint64_t per = total / nthreads, rem = total % nthreads;
+  std::vector<std::thread> pool;
+  uint64_t cursor = begin;
+  for (int t = 0; t < nthreads; ++t) {
+    uint64_t lo = cursor;
+    cursor += per + ((uint64_t)t < rem ? 1 : 0);
+    uint64_t hi = cursor;
+    pool.emplace_back([&, t, lo, hi]() {
+      for (uint64_t s = lo; s < hi; ++s)
+        if (energy_state_bits(flat, n, s) == emin) found[t].push_back(s);
+    });
+  }
+  for (auto &th : pool) th.join();
+  uint64_t count = 0;
+  for (auto &v : found)
+    for (uint64_t s : v) {
+      if (count < cap) states[count] = s;
+      ++count;
+    }
+  *e_out = emin;
+  return count;
+}
+
+// Deterministic verification transcription of sa::anneal's kernel body,
+// include/simulated_annealing/annealing.hpp:87-125, for one trajectory per
+// row of the precomputed arrays.
+//
+// The reference draws from oneMKL philox4x32x10 (annealing.hpp:87), which
+// is not reproducible here. Verification mode instead consumes caller-given
+// arrays: init[t*n + i] (the bit() draws of annealing.hpp:91-93),
+// site[t*steps + a] (bit_index(), :101) and u[t*steps + a] (uniform(),
+// :108), with steps = num_iter * sweeps_per_beta. One (site, u) pair is
+// consumed per attempt unconditionally, so the array index of attempt a is
+// fixed; the reference only draws u when new_energy >= current_energy (the
+// short-circuit at :106-108), which leaves the decisions unchanged.
+//
+// acceptance 0 = the reference rule exp((E_cur - E_new) / beta) > u
+// (:106-108); acceptance 1 = the physical Metropolis rule
+// exp(-beta * (E_new - E_cur)) > u. Energies are full FP64 recomputations
+// per attempt as in the reference (:104).
+//
+// Outputs: best_states/best_energies (the kernel's best_states /
+// best_energies_acc, :115-121,124), final_states/final_energies (the
+// current_states at exit), and accept_count per trajectory.
+void orc_anneal_verify(const double *flat, int n, const double *beta,
+                       int num_iter, int num_tries, int sweeps_per_beta,
+                       const char *init, const int *site, const double *u,
+                       int acceptance, char *best_states,
+                       double *best_energies, char *final_states,
+                       double *final_energies, int64_t *accept_count) {
+  const int64_t steps = (int64_t)num_iter * sweeps_per_beta;
+  for (int t = 0; t < num_tries; ++t) {
+    std::vector<char> cur(init + (size_t)t * n, init + (size_t)(t + 1) * n);
+    std::vector<char> best = cur;
+    double best_energy = energy_ref(flat, cur.data(), n);
+    double current_energy = best_energy;
+    int64_t acc = 0;
+    for (int iter = 0; iter < num_iter; iter++) {
+      double b = beta[iter];
+      for (int sweep = 0; sweep < sweeps_per_beta; sweep++) {
+        int64_t a = (int64_t)iter * sweeps_per_beta + sweep;
+        int k = site[(size_t)t * steps + a];
+        double uu = u[(size_t)t * steps + a];
+        cur[k] = 1 - cur[k];
+        double new_energy = energy_ref(flat, cur.data(), n);
+        bool accept;
+        if (new_energy < current_energy) {
+          accept = true;
+        } else if (acceptance == 0) {
+          accept = std::exp((current_energy - new_energy) / b) > uu;
+        } else {
+          accept = std::exp(-b * (new_energy - current_energy)) > uu;
+        }
+        if (accept) {
+          current_energy = new_energy;
+          ++acc;
+        } else {
+          cur[k] = 1 - cur[k];
+        }
+        if (current_energy < best_energy) {
+          best_energy = current_energy;
+          best = cur;
+        }
+      }
+    }
+    std::memcpy(best_states + (size_t)t * n, best.data(), n);
+    best_energies[t] = best_energy;
+    if (final_states) std::memcpy(final_states + (size_t)t * n, cur.data(), n);
+    if (final_energies) final_energies[t] = current_energy;
+    if (accept_count) accept_count[t] = acc;
+  }
+}
+
+// Free-running CPU anneal with the reference algorithm (full FP64 energy
+// recomputation per attempt, annealing.hpp:97-123) and a host RNG, threaded
+// over trajectories the way the SYCL cpu device runs work-items. Used as the
+// statistical reference (KS tests) and as the timed CPU baseline.
+//
+// site_order 0 = one uniformly random site per step (the reference);
+// site_order 1 = one step is a sequential pass over sites 0..n-1 (n
+// attempts), the physics "sweep". Returns total attempts performed.
+int64_t orc_anneal_free(const double *flat, int n, const double *beta,
+                        int num_iter, int num_tries, int sweeps_per_beta,
+                        uint64_t seed, int acceptance, int site_order,
+                        int nthreads, char *best_states,
+                        double *best_energies) {
+  if (nthreads < 1) nthreads = 1;
+  std::atomic<int> next{0};
+  std::atomic<int64_t> attempts{0};
+  auto worker = [&]() {
+    for (;;) {
+      int t = next.fetch_add(1);
+      if (t >= num_tries) break;
+      HostRng rng(seed * 0x9E3779B97F4A7C15ull + (uint64_t)t * 0xD1B54A32D192ED03ull + 1);
+      std::vector<char> cur(n), best(n);
+      for (int i = 0; i < n; ++i) cur[i] = (char)(rng.next() >> 63);
+      best = cur;
+      double best_energy = energy_ref(flat, cur.data(), n);
+      double current_energy = best_energy;
+      int64_t local = 0;
+      for (int iter = 0; iter < num_iter; iter++) {
+        double b = beta[iter];
+        for (int sweep = 0; sweep < sweeps_per_beta; sweep++) {
+          int inner = site_order == 1 ? n : 1;
+          for (int s = 0; s < inner; ++s) {
+            int k = site_order == 1 ? s : rng.below(n);
+            cur[k] = 1 - cur[k];
+            double new_energy = energy_ref(flat, cur.data(), n);
+            bool accept;
+            if (new_energy < current_energy) {
+              accept = true;
+            } else {
+              double uu = rng.uniform();
+              accept = acceptance == 0
+                           ? std::exp((current_energy - new_energy) / b) > uu
+                           : std::exp(-b * (new_energy - current_energy)) > uu;
+            }
+            if (accept) current_energy = new_energy;
+            else cur[k] = 1 - cur[k];
+            if (current_energy < best_energy) {
+              best_energy = current_energy;
+              best = cur;
+            }
+            ++local;
+          }
+        }
+      }
+      std::memcpy(best_states + (size_t)t * n, best.data(), n);
+      best_energies[t] = best_energy;
+      attempts += local;
+    }
+  };
+  std::vector<std::thread> pool;
+  for (int i = 0; i < nthreads; ++i) pool.emplace_back(worker);
+  for (auto &th : pool) th.join();
+  return attempts.load();
+}
+
+// Host-side argmin over trajectories, annealing.hpp:134-139 (first minimum).
+int orc_argmin(const double *e, int m) {
+  return (int)(std::min_element(e, e + m) - e);
+}
+
+void orc_philox4x32_10(const uint32_t *ctr, const uint32_t *key, uint32_t *out) {
+  philox4x32_10(ctr, key, out);
+}
+
+// qubo::Solution::save, include/model/solution.hpp:58-67: the header row of
+// variable indices followed by "energy", then the 0/1 values and the energy
+// at the default ostream precision (6 significant digits, "%g"). Returns the
+// number of bytes written (excluding the terminator) or -1 if cap is short.
+int orc_solution_csv(const char *state, int n, double energy, char *out, int cap) {
+  std::string s;
+  for (int i = 0; i < n; ++i) s += std::to_string(i) + ",";
+  s += "energy\n";
+  for (int i = 0; i < n; ++i) s += std::to_string((int)state[i]) + ",";
+  char buf[64];
+  std::snprintf(buf, sizeof buf, "%g", energy);
+  s += buf;
+  s += "\n";
+  if ((int)s.size() + 1 > cap) return -1;
+  std::memcpy(out, s.c_str(), s.size() + 1);
+  return (int)s.size();
+}
+
+}  // extern "C"
