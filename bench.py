@@ -512,7 +512,12 @@ def main():
     import onesolver_gb300 as osg
     torch.cuda.set_device(local)
     ctx = osg.Context(local)
-    ctx.set_stream(torch.cuda.current_stream().cuda_stream)
+    # One explicit stream for the library's kernels, the L2 flush and the
+    # timing events (the legacy default stream has handle 0, which the C ABI
+    # reads as "use the context's own stream").
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    ctx.set_stream(stream.cuda_stream)
 
     if args.workload == "exhaustive36":
         out = bench_exhaustive(args, ctx, pg, rank, world)

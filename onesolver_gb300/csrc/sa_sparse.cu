@@ -290,6 +290,7 @@ void plan_create_sparse(os_sa_plan *p, const os_qubo_csr *q) {
   OS_REQUIRE(q && q->row_ptr && q->diag, "null CSR");
   const int n = q->n;
   OS_REQUIRE(n >= 1, "empty instance");
+  OS_REQUIRE(p->T <= 65535, "sparse annealing runs at most 65535 trajectories per call");
   OS_REQUIRE(q->row_ptr[0] == 0, "row_ptr[0] must be 0");
   const int nnz = q->row_ptr[n];
   OS_REQUIRE(nnz >= 0 && (nnz == 0 || (q->col && q->val)), "bad CSR arrays");
