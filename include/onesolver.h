@@ -187,6 +187,29 @@ int32_t os_exhaustive_plan_launches(const os_exh_plan *plan);
 os_status os_exhaustive_plan_kernel_ms(os_exh_plan *plan, float *ms);
 void os_exhaustive_plan_destroy(os_exh_plan *plan);
 
+/* Exhaustive search that allocates no device memory. No counterpart in the
+ * reference. For callers that cannot call cudaMalloc: a process that reserves
+ * the whole device memory for its own pool at start-up, or a latency-critical
+ * path where cudaMalloc / cudaFree would synchronise the device and stall
+ * other streams. All device scratch lives in one file-scope array of
+ * OS_NOALLOC_SCRATCH_BYTES that every GPU loading this library holds until
+ * the process exits; inputs and outputs are the caller's host buffers, as in
+ * os_exhaustive_run, and the work runs on `stream` (a cudaStream_t, NULL =
+ * the legacy default stream) of the current device.
+ *   - Integer coefficients only (int32 or int64 enumeration); non-integer
+ *     instances return OS_INVALID_ARG (use os_exhaustive_run).
+ *   - n <= 50 and max_minimisers <= OS_NOALLOC_MAX_MINIMISERS; larger
+ *     requests return OS_INVALID_ARG.
+ *   - The first call on a device looks up the array's device address
+ *     (cudaGetSymbolAddress); make that first call before any stream
+ *     capture.
+ *   - Every call reuses the same array, so calls whose work overlaps on the
+ *     GPU (other host threads, other streams) race; serialise them. */
+#define OS_NOALLOC_SCRATCH_BYTES (3u << 20)
+#define OS_NOALLOC_MAX_MINIMISERS 65536
+os_status os_exhaustive_run_noalloc(const os_qubo_dense *qubo, const os_exh_params *params,
+                                    os_exh_result *result, void *stream);
+
 /* ------------------------------------------------------------------------ */
 /* Simulated annealing                                                      */
 /* ------------------------------------------------------------------------ */

@@ -120,6 +120,8 @@ SIGNATURES = {
     "os_exhaustive_plan_launches": (C.c_int32, [_P]),
     "os_exhaustive_plan_destroy": (None, [_P]),
     "os_exhaustive_plan_kernel_ms": (C.c_int, [_P, C.POINTER(C.c_float)]),
+    "os_exhaustive_run_noalloc": (C.c_int, [C.POINTER(_QuboDense), C.POINTER(_ExhParams), C.POINTER(_ExhResult),
+                                            _P]),
     "os_sa_run": (C.c_int, [_P, C.POINTER(_QuboDense), C.POINTER(_SaParams), C.POINTER(_SaResult)]),
     "os_sa_run_sparse": (C.c_int, [_P, C.POINTER(_QuboCsr), C.POINTER(_SaParams), C.POINTER(_SaResult)]),
     "os_sa_verify": (C.c_int, [_P, C.POINTER(_QuboDense), C.POINTER(C.c_double), C.c_int32, C.c_int32,

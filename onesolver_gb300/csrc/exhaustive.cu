@@ -852,3 +852,230 @@ os_status os_exhaustive_run(os_ctx *ctx, const os_qubo_dense *qubo, const os_exh
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Exhaustive search without device allocation.
+//
+// For callers that cannot call cudaMalloc: a serving process that reserves
+// the whole device memory for its own pool at start-up, or code on a
+// latency-critical path where cudaMalloc / cudaFree would synchronise the
+// device and stall every other stream. This entry point keeps every piece of
+// device scratch it needs (coefficients, step constants, work counter, CTA
+// records, kept minimisers, summary) in one file-scope array of
+// OS_NOALLOC_SCRATCH_BYTES, which every GPU that loads this library holds
+// until the process exits, and copies the caller's host inputs and outputs
+// in and out of it. It runs the same enumeration kernels as
+// os_exhaustive_run.
+// ---------------------------------------------------------------------------
+
+#include <mutex>
+
+namespace os {
+namespace exh {
+
+constexpr size_t NOALLOC_BYTES = OS_NOALLOC_SCRATCH_BYTES;
+constexpr int NOALLOC_MAX_CTAS = 2048;
+constexpr unsigned long long NOALLOC_MAX_OUT = OS_NOALLOC_MAX_MINIMISERS;
+constexpr int NOALLOC_MAX_DEVICES = 64;
+
+// Section offsets inside the scratch array (256-byte aligned).
+constexpr size_t align256(size_t v) { return (v + 255) & ~size_t(255); }
+constexpr size_t NA_COUNTERS = 0;
+constexpr size_t NA_SUMMARY = align256(NA_COUNTERS + C_N * sizeof(unsigned long long));
+constexpr size_t NA_Q = align256(NA_SUMMARY + sizeof(Summary));
+constexpr size_t NA_KF = align256(NA_Q + (size_t)MAX_N * MAX_N * sizeof(long long));
+constexpr size_t NA_REC = align256(NA_KF + INNER * sizeof(long long));
+constexpr size_t NA_CTA_STATES = align256(NA_REC + NOALLOC_MAX_CTAS * sizeof(CtaRecord<long long>));
+constexpr size_t NA_OUT = align256(NA_CTA_STATES + (size_t)NOALLOC_MAX_CTAS * CTA_CAP * sizeof(unsigned long long));
+constexpr size_t NA_END = align256(NA_OUT + NOALLOC_MAX_OUT * sizeof(unsigned long long));
+static_assert(NA_END <= NOALLOC_BYTES, "no-allocation scratch layout exceeds its array");
+
+// The scratch itself. In host code `g_noalloc_scratch` is only a stand-in
+// for the symbol: its device address comes from cudaGetSymbolAddress.
+static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_BYTES];
+
+std::mutex g_noalloc_mutex;
+unsigned char *g_noalloc_ptr[NOALLOC_MAX_DEVICES] = {};
+
+// Device address of the scratch array on the current device, looked up once
+// per device.
+unsigned char *noalloc_scratch(int device) {
+  OS_REQUIRE(device >= 0 && device < NOALLOC_MAX_DEVICES, "device %d out of range", device);
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  if (!g_noalloc_ptr[device]) {
+    void *ptr = nullptr;
+    OS_CUDA(cudaGetSymbolAddress(&ptr, g_noalloc_scratch));
+    g_noalloc_ptr[device] = static_cast<unsigned char *>(ptr);
+  }
+  return g_noalloc_ptr[device];
+}
+
+template <class T>
+void noalloc_run(const os_qubo_dense *qubo, const os_exh_params &prm, os_exh_result *r, int kind,
+                 cudaStream_t s, int device, unsigned char *base) {
+  const int n = qubo->n;
+  const int free_bits = n - prm.fixed_high_bits;
+  const bool small = free_bits < SMALL_FREE;
+  // Host staging on the stack: coefficients and step constants.
+  T q[MAX_N * MAX_N];
+  for (int i = 0; i < n; ++i)
+    for (int j = i; j < n; ++j)
+      q[(size_t)i * n + j] = q[(size_t)j * n + i] = (T)qubo->f[(size_t)i * n + j];
+  GrayParams<T> P{};
+  T kf[INNER] = {};
+  if (!small) {
+    for (int t = 1; t < INNER; ++t) {
+      const int k = ctz_c(t);
+      const int prev = gray_c(t - 1);
+      const bool up = (gray_c(t) >> k) & 1;
+      T b = q[(size_t)k * n + k];
+      for (int j = 0; j < G; ++j)
+        if (j != k && ((prev >> j) & 1)) b += q[(size_t)k * n + j];
+      kf[t] = up ? b : -b;
+    }
+  }
+  for (int t = 0; t < INNER; ++t) {
+    P.kf[t] = kf[t];
+    P.kr[t] = -kf[t];
+  }
+  unsigned long long *counters = reinterpret_cast<unsigned long long *>(base + NA_COUNTERS);
+  Summary *summary = reinterpret_cast<Summary *>(base + NA_SUMMARY);
+  T *dq = reinterpret_cast<T *>(base + NA_Q);
+  T *dkf = reinterpret_cast<T *>(base + NA_KF);
+  P.q = dq;
+  P.kf_g = dkf;
+  P.n = n;
+  P.prefix_state = prm.fixed_high_bits ? (prm.prefix << free_bits) : 0ull;
+  P.nstates = 1ull << free_bits;
+  if (!small) {
+    const int outer = free_bits - G;
+    P.loop_bits = std::min(LOOP_BITS, outer);
+    P.item_bits = outer - P.loop_bits;
+  }
+  P.work = counters + C_WORK;
+  P.cta = reinterpret_cast<CtaRecord<T> *>(base + NA_REC);
+  P.cta_states = reinterpret_cast<unsigned long long *>(base + NA_CTA_STATES);
+  P.summary = summary;
+  P.window = 0;
+  P.out_count = counters + C_OUT_COUNT;
+  P.out_pos = counters + C_OUT_POS;
+  P.out_states = reinterpret_cast<unsigned long long *>(base + NA_OUT);
+  P.out_minstate = counters + C_OUT_MIN;
+  const unsigned long long user_cap = prm.max_minimisers;
+  P.out_cap = std::max<unsigned long long>(user_cap, 1ull);
+
+  int ctas;
+  if (small) {
+    ctas = (int)ceil_div_u64(P.nstates, THREADS);
+  } else {
+    int occ = 0, sms = 0;
+    OS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, gray_kernel<T, false>, THREADS, 0));
+    OS_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+    const unsigned long long want = ceil_div_u64(1ull << P.item_bits, THREADS);
+    ctas = (int)std::min<unsigned long long>(want, (unsigned long long)sms * std::max(occ, 1));
+    ctas = std::max(1, std::min(ctas, NOALLOC_MAX_CTAS));
+  }
+  OS_REQUIRE(ctas <= NOALLOC_MAX_CTAS, "too many CTAs for the no-allocation scratch");
+
+  // Every call shares the array: clear what must start at zero.
+  OS_CUDA(cudaMemcpyAsync(dq, q, sizeof(T) * n * n, cudaMemcpyHostToDevice, s));
+  OS_CUDA(cudaMemcpyAsync(dkf, kf, sizeof(T) * INNER, cudaMemcpyHostToDevice, s));
+  OS_CUDA(cudaMemsetAsync(counters, 0, C_N * sizeof(unsigned long long), s));
+  OS_CUDA(cudaMemsetAsync(counters + C_OUT_MIN, 0xff, sizeof(unsigned long long), s));
+  if (small) {
+    small_kernel<T, false><<<ctas, THREADS, 0, s>>>(P);
+  } else {
+    gray_kernel<T, false><<<ctas, THREADS, 0, s>>>(P);
+  }
+  OS_CUDA(cudaGetLastError());
+  gather_kernel<T><<<1, 1024, 0, s>>>(P.cta, ctas, P.cta_states, summary, P.out_states, P.out_cap);
+  OS_CUDA(cudaGetLastError());
+  Summary sum;
+  OS_CUDA(cudaMemcpyAsync(&sum, summary, sizeof sum, cudaMemcpyDeviceToHost, s));
+  OS_CUDA(cudaStreamSynchronize(s));
+  unsigned long long count = sum.count, written = sum.collected, minstate = sum.minstate;
+  int passes = 1;
+  if (sum.ovf) {
+    passes = 2;
+    OS_CUDA(cudaMemsetAsync(counters, 0, C_N * sizeof(unsigned long long), s));
+    OS_CUDA(cudaMemsetAsync(counters + C_OUT_MIN, 0xff, sizeof(unsigned long long), s));
+    if (small)
+      small_kernel<T, true><<<ctas, THREADS, 0, s>>>(P);
+    else
+      gray_kernel<T, true><<<ctas, THREADS, 0, s>>>(P);
+    OS_CUDA(cudaGetLastError());
+    unsigned long long c3[3];
+    OS_CUDA(cudaMemcpyAsync(c3, counters + C_OUT_COUNT, sizeof c3, cudaMemcpyDeviceToHost, s));
+    OS_CUDA(cudaStreamSynchronize(s));
+    count = c3[0];
+    written = std::min<unsigned long long>(c3[1], P.out_cap);
+    minstate = c3[2];
+  }
+  const unsigned long long k = std::min<unsigned long long>(written, user_cap);
+  if (r->states && k) {
+    OS_CUDA(cudaMemcpyAsync(r->states, P.out_states, sizeof(unsigned long long) * k,
+                            cudaMemcpyDeviceToHost, s));
+    OS_CUDA(cudaStreamSynchronize(s));
+    std::sort(r->states, r->states + k);
+  }
+  r->energy = (double)sum.gmin;
+  r->state = minstate;
+  r->count = count;
+  r->states_enumerated = 1ull << free_bits;
+  r->coef_kind_used = kind;
+  r->collect_passes = passes;
+}
+
+}  // namespace exh
+}  // namespace os
+
+extern "C" os_status os_exhaustive_run_noalloc(const os_qubo_dense *qubo, const os_exh_params *params,
+                                               os_exh_result *result, void *stream) {
+  os_status extra = OS_OK;
+  os_status st = guard([&] {
+    OS_REQUIRE(qubo && qubo->f && result, "null argument");
+    const int n = qubo->n;
+    OS_REQUIRE(n >= 1 && n <= MAX_N, "exhaustive search supports 1..%d variables (got %d)", MAX_N, n);
+    os_exh_params prm{};
+    if (params) prm = *params;
+    OS_REQUIRE(prm.fixed_high_bits >= 0 && prm.fixed_high_bits < n, "fixed_high_bits must be in [0, n)");
+    if (prm.fixed_high_bits > 0)
+      OS_REQUIRE(prm.prefix < (1ull << prm.fixed_high_bits), "prefix does not fit in fixed_high_bits");
+    else
+      OS_REQUIRE(prm.prefix == 0, "prefix given without fixed_high_bits");
+    OS_REQUIRE(prm.max_minimisers <= NOALLOC_MAX_OUT,
+               "max_minimisers %llu exceeds the no-allocation limit of %llu",
+               (unsigned long long)prm.max_minimisers, (unsigned long long)NOALLOC_MAX_OUT);
+    bool integral = true;
+    double abs_sum = 0.0;
+    for (int i = 0; i < n; ++i)
+      for (int j = i; j < n; ++j) {
+        const double v = qubo->f[(size_t)i * n + j];
+        OS_REQUIRE(std::isfinite(v), "coefficient (%d,%d) is not finite", i, j);
+        integral = integral && v == std::floor(v);
+        abs_sum += std::fabs(v);
+      }
+    int kind = prm.coef_kind;
+    if (kind == OS_COEF_AUTO) kind = !integral ? OS_COEF_FIXED64 : abs_sum < 2147483000.0 ? OS_COEF_INT32 : OS_COEF_INT64;
+    OS_REQUIRE(kind == OS_COEF_INT32 || kind == OS_COEF_INT64,
+               "the no-allocation entry point enumerates integer coefficients only (int32 or int64); "
+               "use os_exhaustive_run for non-integer coefficients");
+    OS_REQUIRE(integral && (kind == OS_COEF_INT64 ? abs_sum < 9.0e15 : abs_sum < 2147483000.0),
+               "coefficients are not exact in the requested integer type");
+    int device = 0;
+    OS_CUDA(cudaGetDevice(&device));
+    unsigned char *base = noalloc_scratch(device);
+    cudaStream_t s = (cudaStream_t)stream;
+    if (kind == OS_COEF_INT32)
+      noalloc_run<int>(qubo, prm, result, kind, s, device, base);
+    else
+      noalloc_run<long long>(qubo, prm, result, kind, s, device, base);
+    if (prm.max_minimisers > 0 && result->count > prm.max_minimisers) extra = OS_OVERFLOW_MINIMISERS;
+  });
+  if (st != OS_OK) return st;
+  if (extra != OS_OK)
+    return fail(extra, "the degenerate set holds %llu states; only %llu fit the buffer",
+                (unsigned long long)result->count,
+                (unsigned long long)(params ? params->max_minimisers : 0));
+  return OS_OK;
+}
