@@ -9,7 +9,8 @@
 // Here the 2^n states are enumerated in Gray-code order so that consecutive
 // states differ in one bit and the energy changes by one precomputed delta:
 //
-//   * the low G = 9 bits ("inner" bits) are walked by fully unrolled code.
+//   * the low G bits ("inner" bits, G = 8..10, 9 by default) are walked by
+//     fully unrolled code.
 //     For step t of the inner Gray sequence the flipped bit k = ctz(t) and
 //     its direction are compile-time constants, so the energy update is
 //       E += K[t] +/- c[k]
@@ -17,8 +18,10 @@
 //     plus its diagonal term) sits in the kernel-parameter constant bank and
 //     c[k] (the coupling of bit k to the current outer bits) in a register:
 //     one three-input integer add and one integer min per state;
-//   * odd blocks walk the inner sequence backwards (the reflected Gray code),
-//     with the negated constants;
+//   * every block walks the same forward sequence, which ends with only the
+//     top inner bit set; one more add clears that bit (back to the block's
+//     first state, not counted twice) so all blocks start from inner state 0
+//     and one copy of the unrolled code serves them all;
 //   * between blocks one outer bit flips; its energy delta is a row sum over
 //     the set bits and the G inner couplings c[] are updated (O(n) work per
 //     2^G states);
@@ -44,13 +47,15 @@
 #include <vector>
 
 #include "common.cuh"
+#include "philox.cuh"
 #include "rescore.cuh"
 
 namespace os {
 namespace exh {
 
-constexpr int G = 9;                 // inner (unrolled) bits
-constexpr int INNER = 1 << G;        // states per block
+constexpr int G_DEFAULT = 10;        // inner (unrolled) bits
+constexpr int G_MAX = 10;
+constexpr int INNER_MAX = 1 << G_MAX;
 constexpr int LCAP = 4;              // states kept per thread
 constexpr int THREADS = 256;         // threads per CTA
 constexpr int CTA_CAP = 128;         // states kept per CTA
@@ -84,8 +89,7 @@ struct Summary {
 };
 
 template <class T> struct GrayParams {
-  T kf[INNER];                    // forward inner step constants (kf[0] unused)
-  T kr[INNER];                    // kr[t] = -kf[t] for the reflected walk
+  T kf[INNER_MAX];                // inner step constants (kf[0] unused)
   const T *q;                     // n x n symmetric coefficients
   const T *kf_g;                  // global copy of kf (slow path)
   int n;                          // row length (all variables)
@@ -95,6 +99,10 @@ template <class T> struct GrayParams {
   unsigned long long prefix_state;  // fixed top bits, in place
   unsigned long long nstates;     // small kernel: states enumerated
   unsigned long long *work;       // work-queue counter
+  long long *gbest;               // best energy found so far (pruning bound)
+  uint32_t seed;                  // descent starting points
+  unsigned long long fixed_mask;  // variables fixed by the shard prefix
+  unsigned long long var_mask;    // (1 << n) - 1
   CtaRecord<T> *cta;              // one record per CTA
   unsigned long long *cta_states; // CTA_CAP per CTA
   // collection pass
@@ -112,30 +120,24 @@ template <> __device__ __forceinline__ int tmax<int>() { return INT_MAX; }
 template <> __device__ __forceinline__ long long tmax<long long>() { return LLONG_MAX; }
 
 // One unrolled inner step; t, k and the direction are template constants.
-template <class T, bool FWD, int I>
-__device__ __forceinline__ void inner_step(T &E, T &m, const T (&c)[G],
-                                           const GrayParams<T> &P) {
-  constexpr int t = FWD ? I : INNER - I;
+template <class T, int G, int t>
+__device__ __forceinline__ void inner_step(T &E, T &m, const T (&c)[G], const GrayParams<T> &P) {
   constexpr int k = ctz_c(t);
   constexpr bool up = (gray_c(t) >> k) & 1;
-  if (FWD)
-    E += P.kf[t] + (up ? c[k] : -c[k]);
-  else
-    E += P.kr[t] + (up ? -c[k] : c[k]);
+  E += P.kf[t] + (up ? c[k] : -c[k]);
   m = min(m, E);
 }
 
-template <class T, bool FWD, int... Is>
-__device__ __forceinline__ void inner_block_impl(T &E, T &m, const T (&c)[G],
-                                                 const GrayParams<T> &P,
+template <class T, int G, int... Is>
+__device__ __forceinline__ void inner_block_impl(T &E, T &m, const T (&c)[G], const GrayParams<T> &P,
                                                  std::integer_sequence<int, Is...>) {
-  (inner_step<T, FWD, Is + 1>(E, m, c, P), ...);
+  (inner_step<T, G, Is + 1>(E, m, c, P), ...);
 }
 
-template <class T, bool FWD>
-__device__ __forceinline__ void inner_block(T &E, T &m, const T (&c)[G],
-                                            const GrayParams<T> &P) {
-  inner_block_impl<T, FWD>(E, m, c, P, std::make_integer_sequence<int, INNER - 1>{});
+// The 2^G - 1 inner steps of one block, from inner state 0.
+template <class T, int G>
+__device__ __forceinline__ void inner_block(T &E, T &m, const T (&c)[G], const GrayParams<T> &P) {
+  inner_block_impl<T, G>(E, m, c, P, std::make_integer_sequence<int, (1 << G) - 1>{});
 }
 
 // Energy of a full state from scratch (set-bit pairs).
@@ -168,7 +170,7 @@ template <class T> struct ThreadBest {
 
 // Inner couplings passed by value to the slow path, so that the hot loop's
 // copy never has its address taken and stays in registers.
-template <class T> struct CVec {
+template <class T, int G> struct CVec {
   T v[G];
 };
 
@@ -203,37 +205,73 @@ __device__ __forceinline__ void collect_state(CollectState &cs, const GrayParams
   }
 }
 
+// Greedy descent from a random state: repeatedly flip the single variable
+// that lowers the energy most, until none does. The energy reached is that
+// of a real state, so it is a valid upper bound on the minimum; it seeds the
+// per-thread pruning bound so that blocks are walked again only when they
+// reach the best energy known (a warp pays for the slow walk whenever any of
+// its lanes needs it).
+template <class T>
+__device__ __noinline__ T descent_bound(const GrayParams<T> &P, uint32_t tid) {
+  const int n = P.n;
+  const T *__restrict__ q = P.q;
+  const Philox4 r = philox4x32_10(tid, 0u, 0u, 0xE5000000u, P.seed, 0x9E3779B9u);
+  const unsigned long long rnd = ((unsigned long long)r.x << 32) | r.y;
+  unsigned long long x = P.prefix_state | (rnd & ~P.fixed_mask & P.var_mask);
+  T h[MAX_N];
+  for (int j = 0; j < n; ++j) {
+    T a = 0;
+    for (int i = 0; i < n; ++i)
+      if (i != j && ((x >> i) & 1ull)) a += q[(size_t)j * n + i];
+    h[j] = a;
+  }
+  T E = energy_from_scratch(q, n, x);
+  for (int it = 0; it < 4 * n; ++it) {
+    T best_d = 0;
+    int best_i = -1;
+    for (int i = 0; i < n; ++i) {
+      if ((P.fixed_mask >> i) & 1ull) continue;
+      const T loc = q[(size_t)i * n + i] + h[i];
+      const T d = ((x >> i) & 1ull) ? -loc : loc;
+      if (d < best_d) {
+        best_d = d;
+        best_i = i;
+      }
+    }
+    if (best_i < 0) break;
+    const bool was = (x >> best_i) & 1ull;
+    x ^= 1ull << best_i;
+    E += best_d;
+    for (int j = 0; j < n; ++j)
+      if (j != best_i) h[j] += was ? -q[(size_t)best_i * n + j] : q[(size_t)best_i * n + j];
+  }
+  return E;
+}
+
 // Slow path: walk one block again, state by state.
-template <class T, bool COLLECT>
-__device__ __noinline__ void revisit_block(const GrayParams<T> &P, const CVec<T> c,
-                                           unsigned long long x_outer, bool odd,
-                                           T Estart, ThreadBest<T> &tb,
+template <class T, int G, bool COLLECT>
+__device__ __noinline__ void revisit_block(const GrayParams<T> &P, const CVec<T, G> c,
+                                           unsigned long long x_outer, T Estart, ThreadBest<T> &tb,
                                            CollectState &cs, T thr) {
   T e = Estart;
-  unsigned long long s = x_outer | (odd ? (1ull << (G - 1)) : 0ull);
+  unsigned long long s = x_outer;
   if (COLLECT) collect_state(cs, P, s, e, thr); else note_state(tb, s, e);
-  for (int i = 1; i < INNER; ++i) {
-    const int t = odd ? INNER - i : i;
+  for (int t = 1; t < (1 << G); ++t) {
     const int k = __ffs(t) - 1;
     const bool up = ((t ^ (t >> 1)) >> k) & 1;
     T ck = 0;
 #pragma unroll
     for (int j = 0; j < G; ++j)
       if (j == k) ck = c.v[j];
-    const T kv = P.kf_g[t];
-    if (!odd)
-      e += kv + (up ? ck : -ck);
-    else
-      e += -kv + (up ? -ck : ck);
+    e += P.kf_g[t] + (up ? ck : -ck);
     s ^= 1ull << k;
     if (COLLECT) collect_state(cs, P, s, e, thr); else note_state(tb, s, e);
   }
 }
 
-template <class T, bool COLLECT>
-__device__ __forceinline__ void process_item(unsigned long long item,
-                                             const GrayParams<T> &P, ThreadBest<T> &tb,
-                                             CollectState &cs, T thr) {
+template <class T, int G, bool COLLECT>
+__device__ __forceinline__ void process_item(unsigned long long item, const GrayParams<T> &P,
+                                             ThreadBest<T> &tb, CollectState &cs, T thr) {
   const int n = P.n;
   const T *__restrict__ q = P.q;
   unsigned long long x = P.prefix_state | (item << (G + P.loop_bits));
@@ -251,33 +289,42 @@ __device__ __forceinline__ void process_item(unsigned long long item,
       for (int i = 0; i < G; ++i) c[i] += row[i];
     }
   }
+  const T top_diag = q[(size_t)(G - 1) * n + (G - 1)];
   const unsigned nblocks = 1u << P.loop_bits;
   for (unsigned B = 0; B < nblocks; ++B) {
     const T Estart = E;
     T m = E;
-    const bool odd = B & 1u;
-    if (!odd)
-      inner_block<T, true>(E, m, c, P);
-    else
-      inner_block<T, false>(E, m, c, P);
+    inner_block<T, G>(E, m, c, P);
+    if (!COLLECT && (B & 7u) == 7u) {
+      // Tighten the bound with the best energy any thread has published.
+      const long long g = *reinterpret_cast<volatile long long *>(P.gbest);
+      if (g < (long long)tb.best) {
+        tb.best = (T)g;
+        tb.cnt = 0;
+        tb.minstate = ~0ull;
+      }
+    }
     if (COLLECT ? (m <= thr) : (m <= tb.best)) {
       if (!COLLECT && m < tb.best) {
         tb.best = m;
         tb.cnt = 0;
         tb.minstate = ~0ull;
+        atomicMin(P.gbest, (long long)m);
       }
-      CVec<T> cv;
+      CVec<T, G> cv;
 #pragma unroll
       for (int i = 0; i < G; ++i) cv.v[i] = c[i];
-      revisit_block<T, COLLECT>(P, cv, x, odd, Estart, tb, cs, thr);
+      revisit_block<T, G, COLLECT>(P, cv, x, Estart, tb, cs, thr);
     }
     if (B + 1 < nblocks) {
+      // Clear the top inner bit (the block ends at inner state 1 << (G-1)),
+      // then flip outer bit G + ctz(B+1) from inner state 0.
+      E -= top_diag + c[G - 1];
       const int mb = G + __ffs((int)(B + 1)) - 1;
       const unsigned long long bm = 1ull << mb;
       const bool was = (x & bm) != 0;
       const T *row = q + (size_t)mb * n;
       T sum = row[mb];
-      if (!odd) sum += row[G - 1];  // inner state after a forward block
       unsigned long long r = x & ~bm;
       while (r) {
         int j = __ffsll((long long)r) - 1;
@@ -334,7 +381,7 @@ __device__ __forceinline__ void cta_reduce(const GrayParams<T> &P, ThreadBest<T>
   }
 }
 
-template <class T, bool COLLECT>
+template <class T, int G, bool COLLECT>
 __global__ void __launch_bounds__(THREADS) gray_kernel(const __grid_constant__ GrayParams<T> P) {
   ThreadBest<T> tb;
   tb.best = tmax<T>();
@@ -342,7 +389,21 @@ __global__ void __launch_bounds__(THREADS) gray_kernel(const __grid_constant__ G
   tb.minstate = ~0ull;
   CollectState cs{0ull, ~0ull, false};
   T thr = 0;
-  if (COLLECT) thr = (T)(P.summary->gmin + P.window);
+  if (COLLECT) {
+    thr = (T)(P.summary->gmin + P.window);
+  } else {
+    // Seed the pruning bound: one greedy descent per thread, reduced over
+    // the CTA and published to the global bound.
+    __shared__ long long s_bound;
+    if (threadIdx.x == 0) s_bound = LLONG_MAX;
+    __syncthreads();
+    const T d = descent_bound(P, blockIdx.x * blockDim.x + threadIdx.x);
+    atomicMin(&s_bound, (long long)d);
+    __syncthreads();
+    if (threadIdx.x == 0) atomicMin(P.gbest, s_bound);
+    const long long g = *reinterpret_cast<volatile long long *>(P.gbest);
+    tb.best = (T)min(s_bound, g);
+  }
   const unsigned long long items = 1ull << P.item_bits;
   const int lane = threadIdx.x & 31;
   for (;;) {
@@ -351,7 +412,7 @@ __global__ void __launch_bounds__(THREADS) gray_kernel(const __grid_constant__ G
     base = __shfl_sync(0xffffffffu, base, 0);
     if (base >= items) break;
     const unsigned long long item = base + lane;
-    if (item < items) process_item<T, COLLECT>(item, P, tb, cs, thr);
+    if (item < items) process_item<T, G, COLLECT>(item, P, tb, cs, thr);
   }
   if (COLLECT) {
     if (cs.count) {
@@ -493,6 +554,7 @@ struct os_exh_plan {
   os_ctx *ctx = nullptr;
   int n = 0, fixed = 0, free_bits = 0;
   int kind = OS_COEF_INT32;
+  int G = G_DEFAULT;             // unrolled inner bits
   bool small = false;
   unsigned long long prefix_state = 0;
   int ctas = 0;
@@ -515,33 +577,36 @@ struct os_exh_plan {
 namespace {
 
 // counters layout: [0] work, [1] out_count, [2] out_pos, [3] out_minstate,
-//                  [4] cand_count, [5] cand_pos, [6] cand_minstate
-enum { C_WORK = 0, C_OUT_COUNT, C_OUT_POS, C_OUT_MIN, C_CAND_COUNT, C_CAND_POS, C_CAND_MIN, C_N };
+//                  [4] cand_count, [5] cand_pos, [6] cand_minstate,
+//                  [7] pruning bound (best energy published so far)
+enum { C_WORK = 0, C_OUT_COUNT, C_OUT_POS, C_OUT_MIN, C_CAND_COUNT, C_CAND_POS, C_CAND_MIN, C_GBEST, C_N };
+
+// Inner step constants for width G: kf[t] = +/- (Q_kk + sum of Q_kj over
+// the other inner bits set before step t), k = ctz(t).
+template <class T> void inner_constants(const T *q, int n, int G, T *kf) {
+  for (int t = 0; t < INNER_MAX; ++t) kf[t] = 0;
+  for (int t = 1; t < (1 << G); ++t) {
+    const int k = ctz_c(t);
+    const int prev = gray_c(t - 1);
+    const bool up = (gray_c(t) >> k) & 1;
+    T base = q[(size_t)k * n + k];
+    for (int j = 0; j < G; ++j)
+      if (j != k && ((prev >> j) & 1)) base += q[(size_t)k * n + j];
+    kf[t] = up ? base : -base;
+  }
+}
 
 template <class T>
 void fill_params(os_exh_plan *p, GrayParams<T> &P, const std::vector<T> &q,
                  DevBuf<T> &dq, DevBuf<T> &dkf) {
   const int n = p->n;
-  std::vector<T> kf(INNER, 0);
-  if (!p->small) {
-    for (int t = 1; t < INNER; ++t) {
-      const int k = ctz_c(t);
-      const int prev = gray_c(t - 1);
-      const bool up = (gray_c(t) >> k) & 1;
-      T base = q[(size_t)k * n + k];
-      for (int j = 0; j < G; ++j)
-        if (j != k && ((prev >> j) & 1)) base += q[(size_t)k * n + j];
-      kf[t] = up ? base : -base;
-    }
-  }
+  std::vector<T> kf(INNER_MAX, 0);
+  if (!p->small) inner_constants(q.data(), n, p->G, kf.data());
   dq.alloc(q.size());
   OS_CUDA(cudaMemcpy(dq.get(), q.data(), sizeof(T) * q.size(), cudaMemcpyHostToDevice));
-  dkf.alloc(INNER);
-  OS_CUDA(cudaMemcpy(dkf.get(), kf.data(), sizeof(T) * INNER, cudaMemcpyHostToDevice));
-  for (int t = 0; t < INNER; ++t) {
-    P.kf[t] = kf[t];
-    P.kr[t] = -kf[t];
-  }
+  dkf.alloc(INNER_MAX);
+  OS_CUDA(cudaMemcpy(dkf.get(), kf.data(), sizeof(T) * INNER_MAX, cudaMemcpyHostToDevice));
+  for (int t = 0; t < INNER_MAX; ++t) P.kf[t] = kf[t];
   P.q = dq.get();
   P.kf_g = dkf.get();
   P.n = n;
@@ -551,12 +616,16 @@ void fill_params(os_exh_plan *p, GrayParams<T> &P, const std::vector<T> &q,
     P.item_bits = 0;
     P.nstates = 1ull << p->free_bits;
   } else {
-    const int outer = p->free_bits - G;
+    const int outer = p->free_bits - p->G;
     P.loop_bits = std::min(LOOP_BITS, outer);
     P.item_bits = outer - P.loop_bits;
     P.nstates = 1ull << p->free_bits;
   }
   P.work = p->counters.get() + C_WORK;
+  P.gbest = reinterpret_cast<long long *>(p->counters.get() + C_GBEST);
+  P.seed = 0x5EEDu;
+  P.var_mask = n >= 64 ? ~0ull : ((1ull << n) - 1ull);
+  P.fixed_mask = P.var_mask & ~((1ull << p->free_bits) - 1ull);
   P.cta = reinterpret_cast<CtaRecord<T> *>(p->rec.get());
   P.cta_states = p->cta_states.get();
   P.summary = p->summary.get();
@@ -568,11 +637,30 @@ void fill_params(os_exh_plan *p, GrayParams<T> &P, const std::vector<T> &q,
   P.out_minstate = p->counters.get() + C_OUT_MIN;
 }
 
+// Launch gray_kernel<T, G, COLLECT> for a runtime G.
+template <class T, bool COLLECT>
+void launch_gray(int G, int grid, cudaStream_t s, const GrayParams<T> &P) {
+  switch (G) {
+    case 8: gray_kernel<T, 8, COLLECT><<<grid, THREADS, 0, s>>>(P); break;
+    case 9: gray_kernel<T, 9, COLLECT><<<grid, THREADS, 0, s>>>(P); break;
+    case 10: gray_kernel<T, 10, COLLECT><<<grid, THREADS, 0, s>>>(P); break;
+    default: throw_error(OS_INVALID_ARG, "inner_bits must be 8, 9 or 10");
+  }
+}
+
+template <class T> int gray_occupancy(int G) {
+  int occ = 0;
+  switch (G) {
+    case 8: OS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, gray_kernel<T, 8, false>, THREADS, 0)); break;
+    case 9: OS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, gray_kernel<T, 9, false>, THREADS, 0)); break;
+    default: OS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, gray_kernel<T, 10, false>, THREADS, 0)); break;
+  }
+  return occ < 1 ? 1 : occ;
+}
+
 template <class T> int grid_for(os_exh_plan *p, const GrayParams<T> &P) {
   if (p->small) return (int)ceil_div_u64(P.nstates, THREADS);
-  int occ = 0;
-  OS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, gray_kernel<T, false>, THREADS, 0));
-  if (occ < 1) occ = 1;
+  const int occ = gray_occupancy<T>(p->G);
   const unsigned long long items = 1ull << P.item_bits;
   const unsigned long long want = ceil_div_u64(items, THREADS);
   return (int)std::max<unsigned long long>(1, std::min<unsigned long long>(want, (unsigned long long)p->ctx->sm_count * occ));
@@ -594,9 +682,9 @@ template <class T> void launch_pass(os_exh_plan *p, GrayParams<T> &P, bool colle
       small_kernel<T, false><<<p->ctas, THREADS, 0, s>>>(P);
   } else {
     if (collect)
-      gray_kernel<T, true><<<p->ctas, THREADS, 0, s>>>(P);
+      launch_gray<T, true>(p->G, p->ctas, s, P);
     else
-      gray_kernel<T, false><<<p->ctas, THREADS, 0, s>>>(P);
+      launch_gray<T, false>(p->G, p->ctas, s, P);
   }
   OS_CUDA(cudaGetLastError());
   ++p->launches;
@@ -606,6 +694,7 @@ template <class T> void execute_typed(os_exh_plan *p, GrayParams<T> &P) {
   cudaStream_t s = p->ctx->stream;
   p->launches = 0;
   OS_CUDA(cudaMemsetAsync(p->counters.get() + C_WORK, 0, sizeof(unsigned long long), s));
+  OS_CUDA(cudaMemsetAsync(p->counters.get() + C_GBEST, 0x7f, sizeof(unsigned long long), s));
   OS_CUDA(cudaEventRecord(p->ev0, s));
   launch_pass(p, P, false);
   OS_CUDA(cudaEventRecord(p->ev1, s));
@@ -680,6 +769,8 @@ os_status os_exhaustive_plan_create(os_ctx *ctx, const os_qubo_dense *qubo,
       else kind = OS_COEF_FIXED64;
     }
     OS_REQUIRE(kind >= OS_COEF_INT32 && kind <= OS_COEF_FIXED64, "unknown coef_kind %d", kind);
+    OS_REQUIRE(prm.inner_bits == 0 || (prm.inner_bits >= 8 && prm.inner_bits <= G_MAX),
+               "inner_bits must be 0 (default), 8, 9 or 10");
     if (kind == OS_COEF_INT32)
       OS_REQUIRE(integral && abs_sum < 2147483000.0, "coefficients are not int32-exact");
     if (kind == OS_COEF_INT64)
@@ -693,6 +784,7 @@ os_status os_exhaustive_plan_create(os_ctx *ctx, const os_qubo_dense *qubo,
       p->free_bits = n - prm.fixed_high_bits;
       p->kind = kind;
       p->small = p->free_bits < SMALL_FREE;
+      p->G = prm.inner_bits ? prm.inner_bits : G_DEFAULT;
       p->prefix_state = prm.fixed_high_bits ? (prm.prefix << p->free_bits) : 0ull;
       p->user_cap = prm.max_minimisers;
       p->out_cap = std::max<unsigned long long>(prm.max_minimisers, 1ull);
@@ -884,7 +976,7 @@ constexpr size_t NA_COUNTERS = 0;
 constexpr size_t NA_SUMMARY = align256(NA_COUNTERS + C_N * sizeof(unsigned long long));
 constexpr size_t NA_Q = align256(NA_SUMMARY + sizeof(Summary));
 constexpr size_t NA_KF = align256(NA_Q + (size_t)MAX_N * MAX_N * sizeof(long long));
-constexpr size_t NA_REC = align256(NA_KF + INNER * sizeof(long long));
+constexpr size_t NA_REC = align256(NA_KF + INNER_MAX * sizeof(long long));
 constexpr size_t NA_CTA_STATES = align256(NA_REC + NOALLOC_MAX_CTAS * sizeof(CtaRecord<long long>));
 constexpr size_t NA_OUT = align256(NA_CTA_STATES + (size_t)NOALLOC_MAX_CTAS * CTA_CAP * sizeof(unsigned long long));
 constexpr size_t NA_END = align256(NA_OUT + NOALLOC_MAX_OUT * sizeof(unsigned long long));
@@ -921,23 +1013,12 @@ void noalloc_run(const os_qubo_dense *qubo, const os_exh_params &prm, os_exh_res
   for (int i = 0; i < n; ++i)
     for (int j = i; j < n; ++j)
       q[(size_t)i * n + j] = q[(size_t)j * n + i] = (T)qubo->f[(size_t)i * n + j];
+  constexpr int G = G_DEFAULT;
   GrayParams<T> P{};
-  T kf[INNER] = {};
-  if (!small) {
-    for (int t = 1; t < INNER; ++t) {
-      const int k = ctz_c(t);
-      const int prev = gray_c(t - 1);
-      const bool up = (gray_c(t) >> k) & 1;
-      T b = q[(size_t)k * n + k];
-      for (int j = 0; j < G; ++j)
-        if (j != k && ((prev >> j) & 1)) b += q[(size_t)k * n + j];
-      kf[t] = up ? b : -b;
-    }
-  }
-  for (int t = 0; t < INNER; ++t) {
-    P.kf[t] = kf[t];
-    P.kr[t] = -kf[t];
-  }
+  T kf[INNER_MAX];
+  if (!small) inner_constants(q, n, G, kf);
+  else for (int t = 0; t < INNER_MAX; ++t) kf[t] = 0;
+  for (int t = 0; t < INNER_MAX; ++t) P.kf[t] = kf[t];
   unsigned long long *counters = reinterpret_cast<unsigned long long *>(base + NA_COUNTERS);
   Summary *summary = reinterpret_cast<Summary *>(base + NA_SUMMARY);
   T *dq = reinterpret_cast<T *>(base + NA_Q);
@@ -953,6 +1034,10 @@ void noalloc_run(const os_qubo_dense *qubo, const os_exh_params &prm, os_exh_res
     P.item_bits = outer - P.loop_bits;
   }
   P.work = counters + C_WORK;
+  P.gbest = reinterpret_cast<long long *>(counters + C_GBEST);
+  P.seed = 0x5EEDu;
+  P.var_mask = n >= 64 ? ~0ull : ((1ull << n) - 1ull);
+  P.fixed_mask = P.var_mask & ~((1ull << free_bits) - 1ull);
   P.cta = reinterpret_cast<CtaRecord<T> *>(base + NA_REC);
   P.cta_states = reinterpret_cast<unsigned long long *>(base + NA_CTA_STATES);
   P.summary = summary;
@@ -969,7 +1054,7 @@ void noalloc_run(const os_qubo_dense *qubo, const os_exh_params &prm, os_exh_res
     ctas = (int)ceil_div_u64(P.nstates, THREADS);
   } else {
     int occ = 0, sms = 0;
-    OS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, gray_kernel<T, false>, THREADS, 0));
+    OS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, gray_kernel<T, G, false>, THREADS, 0));
     OS_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
     const unsigned long long want = ceil_div_u64(1ull << P.item_bits, THREADS);
     ctas = (int)std::min<unsigned long long>(want, (unsigned long long)sms * std::max(occ, 1));
@@ -979,13 +1064,14 @@ void noalloc_run(const os_qubo_dense *qubo, const os_exh_params &prm, os_exh_res
 
   // Every call shares the array: clear what must start at zero.
   OS_CUDA(cudaMemcpyAsync(dq, q, sizeof(T) * n * n, cudaMemcpyHostToDevice, s));
-  OS_CUDA(cudaMemcpyAsync(dkf, kf, sizeof(T) * INNER, cudaMemcpyHostToDevice, s));
+  OS_CUDA(cudaMemcpyAsync(dkf, kf, sizeof(T) * INNER_MAX, cudaMemcpyHostToDevice, s));
   OS_CUDA(cudaMemsetAsync(counters, 0, C_N * sizeof(unsigned long long), s));
   OS_CUDA(cudaMemsetAsync(counters + C_OUT_MIN, 0xff, sizeof(unsigned long long), s));
+  OS_CUDA(cudaMemsetAsync(counters + C_GBEST, 0x7f, sizeof(unsigned long long), s));
   if (small) {
     small_kernel<T, false><<<ctas, THREADS, 0, s>>>(P);
   } else {
-    gray_kernel<T, false><<<ctas, THREADS, 0, s>>>(P);
+    gray_kernel<T, G, false><<<ctas, THREADS, 0, s>>>(P);
   }
   OS_CUDA(cudaGetLastError());
   gather_kernel<T><<<1, 1024, 0, s>>>(P.cta, ctas, P.cta_states, summary, P.out_states, P.out_cap);
@@ -1002,7 +1088,7 @@ void noalloc_run(const os_qubo_dense *qubo, const os_exh_params &prm, os_exh_res
     if (small)
       small_kernel<T, true><<<ctas, THREADS, 0, s>>>(P);
     else
-      gray_kernel<T, true><<<ctas, THREADS, 0, s>>>(P);
+      gray_kernel<T, G, true><<<ctas, THREADS, 0, s>>>(P);
     OS_CUDA(cudaGetLastError());
     unsigned long long c3[3];
     OS_CUDA(cudaMemcpyAsync(c3, counters + C_OUT_COUNT, sizeof c3, cudaMemcpyDeviceToHost, s));

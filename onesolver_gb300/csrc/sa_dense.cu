@@ -93,6 +93,13 @@ template <int SLOTS> void launch_seq(const DenseArgs &a, int warps, cudaStream_t
   const int grid = (a.traj_count + warps - 1) / warps;
   sa_dense_seq_kernel<SLOTS><<<grid, warps * 32, 0, s>>>(a);
 }
+template <int SLOTS> void launch_tile(const DenseArgs &a, int warps, cudaStream_t s) {
+  const int grid = (a.traj_count + warps - 1) / warps;
+  const size_t smem = (size_t)2 * TILE_ROWS * a.ld * sizeof(float);
+  OS_CUDA(cudaFuncSetAttribute(sa_dense_tile_kernel<SLOTS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)smem));
+  sa_dense_tile_kernel<SLOTS><<<grid, warps * 32, smem, s>>>(a);
+}
 template <int SLOTS> void launch_rand(const DenseArgs &a, int warps, cudaStream_t s) {
   const int grid = (a.traj_count + warps - 1) / warps;
   sa_dense_rand_kernel<SLOTS><<<grid, warps * 32, 0, s>>>(a);
@@ -114,8 +121,13 @@ template <int SLOTS> void launch_resync(const ResyncArgs &a, int warps, cudaStre
     default: throw_error(OS_INVALID_ARG, "unsupported slot count %d", cls); \
   }
 
+// Largest padded row length whose two 16-row tiles fit in shared memory.
+constexpr int TILE_MAX_LD = 1792;
+
 void dense_sweeps(const DenseArgs &a, int slot_cls, int warps, bool sequential, cudaStream_t s) {
-  if (sequential) {
+  if (sequential && a.ld <= TILE_MAX_LD) {
+    OS_SLOT_DISPATCH(slot_cls, launch_tile, a, warps, s);
+  } else if (sequential) {
     OS_SLOT_DISPATCH(slot_cls, launch_seq, a, warps, s);
   } else {
     OS_SLOT_DISPATCH(slot_cls, launch_rand, a, warps, s);
@@ -124,12 +136,18 @@ void dense_sweeps(const DenseArgs &a, int slot_cls, int warps, bool sequential, 
 }
 
 void dense_resync(const ResyncArgs &a, int slot_cls, int warps, cudaStream_t s) {
+  warps = warps > 4 ? 4 : warps;
   OS_SLOT_DISPATCH(slot_cls, launch_resync, a, warps, s);
   OS_CUDA(cudaGetLastError());
 }
 
-// Warps per CTA: spread small trajectory counts over all SMs.
-int dense_warps(int traj, int sm_count) {
+// Warps (trajectories) per CTA: spread small trajectory counts over all SMs;
+// larger CTAs share each staged coupling tile among more trajectories.
+int dense_warps(int traj, int sm_count, bool tiled) {
+  if (tiled) {
+    int w = (traj + sm_count - 1) / sm_count;
+    return w < 1 ? 1 : (w > 8 ? 8 : w);
+  }
   if (traj <= sm_count * 4) return 1;
   if (traj <= sm_count * 16) return 2;
   return 4;
@@ -164,7 +182,9 @@ void plan_create_dense(os_sa_plan *p, const os_qubo_dense *q) {
   p->accepted.alloc(T);
   p->states.alloc(T * (size_t)hst.n);
   p->e64.alloc(T);
-  p->warps = dense_warps((int)T, p->ctx->sm_count);
+  p->tiled = p->sequential && hst.ld <= TILE_MAX_LD;
+  p->warps = dense_warps((int)T, p->ctx->sm_count, p->tiled);
+  p->status.alloc(1);
 }
 
 void execute_dense(os_sa_plan *p) {
@@ -214,6 +234,8 @@ void execute_dense(os_sa_plan *p) {
   a.e = p->e.get();
   a.ebest = p->ebest.get();
   a.accepted = p->accepted.get();
+  a.status = p->status.get();
+  OS_CUDA(cudaMemsetAsync(p->status.get(), 0, sizeof(int), s));
   r.init = 0;
   const int chunk = p->chunk;
   p->sweep_ev_used = 0;
@@ -273,6 +295,11 @@ os_status os_sa_plan_result(os_sa_plan *p, os_sa_result *res) {
     cudaStream_t s = p->ctx->stream;
     OS_CUDA(cudaStreamSynchronize(s));
     const int T = p->T, n = p->n;
+    if (p->status.count) {
+      int st = 0;
+      OS_CUDA(cudaMemcpy(&st, p->status.get(), sizeof st, cudaMemcpyDeviceToHost));
+      if (st) throw_error(OS_TIMEOUT, "a sweep kernel's bounded wait for a coupling tile ran out");
+    }
     std::vector<double> e(T);
     OS_CUDA(cudaMemcpy(e.data(), p->e64.get(), sizeof(double) * T, cudaMemcpyDeviceToHost));
     std::vector<unsigned long long> acc(T);

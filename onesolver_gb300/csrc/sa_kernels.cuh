@@ -31,6 +31,7 @@
 #include <cstdint>
 
 #include "philox.cuh"
+#include "tma.cuh"
 
 namespace os {
 namespace sa {
@@ -54,6 +55,7 @@ struct DenseArgs {
   float *e;                // [traj] tracked energy
   float *ebest;            // [traj]
   unsigned long long *accepted;  // [traj]
+  int *status;             // set to 1 when a bounded wait ran out
 };
 
 __device__ __forceinline__ float select4(const Philox4 &r, int j) {
@@ -198,6 +200,150 @@ __global__ void __launch_bounds__(128) sa_dense_rand_kernel(const __grid_constan
     a.e[t] = E;
     a.ebest[t] = Eb;
     a.accepted[t] += acc;
+  }
+}
+
+// Sequential sweeps with the coupling rows staged in shared memory.
+//
+// A CTA runs W trajectories (one warp each) of the same instance in lockstep
+// over half-slots of 16 sites. The 16 coupling rows of a half-slot (16 x ld
+// FP32, contiguous in global memory) arrive by one bulk async copy (TMA) into
+// one of two buffers while the previous half-slot is processed, and every
+// warp of the CTA takes its flip rows from that tile: the rows are read from
+// L2 once per CTA instead of once per accepted flip per trajectory, and no
+// flip waits on a global load. Tiles run round-robin through the sweep, so
+// the first tiles of the next sweep stream in during the last ones of the
+// current sweep.
+constexpr int TILE_ROWS = 16;
+constexpr uint32_t TILE_WAIT_LIMIT = 1u << 26;
+
+template <int SLOTS>
+__global__ void __launch_bounds__(256) sa_dense_tile_kernel(const __grid_constant__ DenseArgs a) {
+  extern __shared__ __align__(128) unsigned char tile_smem[];
+  __shared__ __align__(8) uint64_t bar[2];
+  float *tiles = reinterpret_cast<float *>(tile_smem);
+  const int lane = threadIdx.x & 31;
+  const int W = blockDim.x >> 5;
+  const int t = blockIdx.x * W + (threadIdx.x >> 5);
+  const bool active = t < a.traj_count;
+  const int nslots = a.nslots, ld = a.ld;
+  const size_t tile_floats = (size_t)TILE_ROWS * ld;
+  const uint32_t tile_bytes = (uint32_t)(tile_floats * sizeof(float));
+  const int halves = 2 * nslots;
+  const long long total = (long long)(a.step_end - a.step_begin) * halves;
+
+  float h[SLOTS];
+  unsigned long long xl = 0, xb = 0;
+  float E = 0.f, Eb = 0.f;
+  float *hp = a.h + (size_t)t * nslots * 32 + lane;
+  if (active) {
+#pragma unroll
+    for (int s = 0; s < SLOTS; ++s) h[s] = s < nslots ? hp[s * 32] : 0.f;
+    xl = a.x[(size_t)t * 32 + lane];
+    xb = a.xbest[(size_t)t * 32 + lane];
+    E = a.e[t];
+    Eb = a.ebest[t];
+  } else {
+#pragma unroll
+    for (int s = 0; s < SLOTS; ++s) h[s] = 0.f;
+  }
+  unsigned long long acc = 0;
+  const uint32_t tg = (uint32_t)(a.traj_offset + t);
+  const uint32_t c3 = (a.instance & 0x0FFFFFFFu) | kStreamSweep;
+
+  if (threadIdx.x == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    mbar_fence_init();
+  }
+  __syncthreads();
+  auto issue = [&](long long g) {
+    const int hs = (int)(g % halves);
+    const int b = (int)(g & 1);
+    mbar_arrive_expect_tx(&bar[b], tile_bytes);
+    bulk_load(tiles + (size_t)b * tile_floats, a.c + (size_t)hs * TILE_ROWS * ld, tile_bytes, &bar[b]);
+  };
+  if (threadIdx.x == 0) {
+    if (total > 0) issue(0);
+    if (total > 1) issue(1);
+  }
+  uint32_t parity[2] = {0u, 0u};
+  long long g = 0;
+  bool failed = false;
+  for (int step = a.step_begin; step < a.step_end && !failed; ++step) {
+    const float b = (float)a.beta[step / a.spb];
+    Philox4 r{0, 0, 0, 0};
+#pragma unroll
+    for (int s = 0; s < SLOTS; ++s) {
+      if (s >= nslots || failed) break;
+      if ((s & 3) == 0)
+        r = philox4x32_10((uint32_t)((s >> 2) * 32 + lane), (uint32_t)step, tg, c3, a.seed_lo, a.seed_hi);
+      const float theta = threshold(select4(r, s & 3), b, a.acceptance);
+      const int site = s * 32 + lane;
+      const bool valid = site < a.n;
+      const float d = a.diag[site];
+#pragma unroll
+      for (int half = 0; half < 2; ++half) {
+        const bool ok = mbar_wait_bounded(&bar[half], parity[half], TILE_WAIT_LIMIT);
+        parity[half] ^= 1u;
+        if (active && ok) {
+          const float *tile = tiles + (size_t)half * tile_floats;
+          int p = half * TILE_ROWS;
+          const int pend = p + TILE_ROWS;
+          for (;;) {
+            const bool xs = (xl >> s) & 1ull;
+            const float loc = d + h[s];
+            const float dE = xs ? -loc : loc;
+            const unsigned mask = __ballot_sync(FULL, valid && lane >= p && lane < pend && dE < theta);
+            if (!mask) break;
+            const int i = __ffs(mask) - 1;
+            const float dEi = __shfl_sync(FULL, dE, i);
+            const bool xi = __shfl_sync(FULL, xs, i);
+            const float sgn = xi ? -1.f : 1.f;
+            const float *row = tile + (size_t)(i - half * TILE_ROWS) * ld + lane;
+#pragma unroll
+            for (int s2 = 0; s2 < SLOTS; ++s2)
+              if (s2 < nslots) h[s2] = fmaf(sgn, row[s2 * 32], h[s2]);
+            if (lane == i) xl ^= 1ull << s;
+            E += dEi;
+            ++acc;
+            if (E < Eb) {
+              Eb = E;
+              xb = xl;
+            }
+            p = i + 1;
+          }
+        }
+        // Every warp is done with this buffer; refill it with tile g + 2.
+        if (__syncthreads_or(!ok)) {
+          failed = true;
+          break;
+        }
+        if (threadIdx.x == 0 && g + 2 < total) issue(g + 2);
+        ++g;
+      }
+    }
+  }
+  if (failed) {
+    // Let copies still in flight land (bounded) before the CTA's shared
+    // memory is released, and report the timeout.
+    if (threadIdx.x == 0) {
+      for (int b2 = 0; b2 < 2; ++b2) mbar_wait_bounded(&bar[b2], parity[b2], TILE_WAIT_LIMIT);
+      if (a.status) atomicExch(a.status, 1);
+    }
+    return;
+  }
+  if (active) {
+#pragma unroll
+    for (int s = 0; s < SLOTS; ++s)
+      if (s < nslots) hp[s * 32] = h[s];
+    a.x[(size_t)t * 32 + lane] = xl;
+    a.xbest[(size_t)t * 32 + lane] = xb;
+    if (lane == 0) {
+      a.e[t] = E;
+      a.ebest[t] = Eb;
+      a.accepted[t] += acc;
+    }
   }
 }
 

@@ -17,6 +17,8 @@ struct os_sa_plan {
   unsigned long long attempts_per_step = 1;
   int launches = 0;
   int warps = 4;
+  bool tiled = false;
+  os::DevBuf<int> status;                   // bounded-wait failures
   // CUDA events around every sweep launch of the last execute (kernel time)
   std::vector<cudaEvent_t> sweep_ev;
   int sweep_ev_used = 0;

@@ -155,3 +155,15 @@ def test_n36_config(native, orc, ctx):
         e, s = orc.exhaustive(f, p << 22, (p + 1) << 22)
         assert part.energy == e and part.state == s
         assert part.energy >= res.energy
+
+
+@pytest.mark.parametrize("n", [14, 21, 27])
+def test_inner_widths_agree(native, orc, ctx, n):
+    f = random_int_qubo(n, 40 + n, -2, 2)
+    res = [native.exhaustive(f, ctx=ctx, inner_bits=g, max_minimisers=1 << 16) for g in (8, 9, 10)]
+    for r in res[1:]:
+        assert (r.energy, r.state, r.count, r.states.tolist()) == \
+            (res[0].energy, res[0].state, res[0].count, res[0].states.tolist())
+    if n <= 21:
+        e, count, states = orc.exhaustive_all(f)
+        assert res[0].energy == e and res[0].count == count
