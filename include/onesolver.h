@@ -141,8 +141,11 @@ typedef struct os_exh_params {
   int32_t fixed_high_bits;  /* 0 = whole space; k > 0 fixes the top k bits */
   uint64_t prefix;          /* value of the fixed top bits (shard index) */
   uint64_t max_minimisers;  /* capacity of os_exh_result.states */
-  int32_t inner_bits;       /* 0 = default (10); 8..10 sets how many low bits
-                               the unrolled inner loop walks (tuning) */
+  int32_t inner_bits;       /* 0 = default (10); 9 or 10 sets how many low
+                               bits the unrolled inner loop walks (tuning) */
+  int32_t variant;          /* 0 = default; 1 = three-input add + min per
+                               state; 2 = multiply-add + fused add-min
+                               (int32 only; tuning) */
 } os_exh_params;
 
 typedef struct os_exh_result {

@@ -67,7 +67,7 @@ class _QuboCsr(C.Structure):
 
 class _ExhParams(C.Structure):
     _fields_ = [("coef_kind", C.c_int32), ("fixed_high_bits", C.c_int32), ("prefix", C.c_uint64),
-                ("max_minimisers", C.c_uint64), ("inner_bits", C.c_int32)]
+                ("max_minimisers", C.c_uint64), ("inner_bits", C.c_int32), ("variant", C.c_int32)]
 
 
 class _ExhResult(C.Structure):
@@ -356,8 +356,8 @@ class ExhaustiveResult:
         return [(self.state >> i) & 1 for i in range(n)]
 
 
-def _exh_params(coef_kind, fixed_high_bits, prefix, max_minimisers, inner_bits=0) -> _ExhParams:
-    return _ExhParams(coef_kind, fixed_high_bits, prefix, max_minimisers, inner_bits)
+def _exh_params(coef_kind, fixed_high_bits, prefix, max_minimisers, inner_bits=0, variant=0) -> _ExhParams:
+    return _ExhParams(coef_kind, fixed_high_bits, prefix, max_minimisers, inner_bits, variant)
 
 
 def _exh_result(res: _ExhResult, states: np.ndarray, cap: int, status: int) -> ExhaustiveResult:
@@ -368,14 +368,14 @@ def _exh_result(res: _ExhResult, states: np.ndarray, cap: int, status: int) -> E
 
 def exhaustive(f: np.ndarray, *, ctx: Optional[Context] = None, coef_kind: int = COEF_AUTO,
                fixed_high_bits: int = 0, prefix: int = 0, max_minimisers: int = 4096,
-               allow_overflow: bool = False, inner_bits: int = 0) -> ExhaustiveResult:
+               allow_overflow: bool = False, inner_bits: int = 0, variant: int = 0) -> ExhaustiveResult:
     """exhaustive::solve on the GPU: ground energy, reference minimiser, degenerate set."""
     ctx = ctx or default_context()
     q, keep = _dense(f)
     states = np.zeros(max(max_minimisers, 1), dtype=np.uint64)
     res = _ExhResult()
     res.states = states.ctypes.data_as(C.POINTER(C.c_uint64))
-    prm = _exh_params(coef_kind, fixed_high_bits, prefix, max_minimisers, inner_bits)
+    prm = _exh_params(coef_kind, fixed_high_bits, prefix, max_minimisers, inner_bits, variant)
     st = lib().os_exhaustive_run(ctx.handle, C.byref(q), C.byref(prm), C.byref(res))
     if st == OVERFLOW_MINIMISERS and allow_overflow:
         return _exh_result(res, states, max_minimisers, st)
@@ -387,12 +387,13 @@ class ExhaustivePlan:
     """Device-resident exhaustive search (create / execute / result)."""
 
     def __init__(self, f: np.ndarray, *, ctx: Optional[Context] = None, coef_kind: int = COEF_AUTO,
-                 fixed_high_bits: int = 0, prefix: int = 0, max_minimisers: int = 4096, inner_bits: int = 0):
+                 fixed_high_bits: int = 0, prefix: int = 0, max_minimisers: int = 4096, inner_bits: int = 0,
+                 variant: int = 0):
         self.ctx = ctx or default_context()
         q, self._keep = _dense(f)
         self.cap = max_minimisers
         self._h = _P()
-        prm = _exh_params(coef_kind, fixed_high_bits, prefix, max_minimisers, inner_bits)
+        prm = _exh_params(coef_kind, fixed_high_bits, prefix, max_minimisers, inner_bits, variant)
         _check(lib().os_exhaustive_plan_create(self.ctx.handle, C.byref(q), C.byref(prm), C.byref(self._h)))
 
     def execute(self) -> None:

@@ -43,386 +43,16 @@
 #include <algorithm>
 #include <climits>
 #include <cmath>
+#include <type_traits>
 #include <utility>
 #include <vector>
 
 #include "common.cuh"
-#include "philox.cuh"
+#include "exhaustive_kernels.cuh"
 #include "rescore.cuh"
 
 namespace os {
 namespace exh {
-
-constexpr int G_DEFAULT = 10;        // inner (unrolled) bits
-constexpr int G_MAX = 10;
-constexpr int INNER_MAX = 1 << G_MAX;
-constexpr int LCAP = 4;              // states kept per thread
-constexpr int THREADS = 256;         // threads per CTA
-constexpr int CTA_CAP = 128;         // states kept per CTA
-constexpr int LOOP_BITS = 5;         // blocks per work item = 2^LOOP_BITS
-constexpr int SMALL_FREE = 14;       // below: one thread per state
-constexpr int MAX_N = 50;
-constexpr uint64_t CAND_CAP = 1u << 20;  // fixed-point candidate buffer
-
-__host__ __device__ constexpr int ctz_c(int t) {
-  int k = 0;
-  while (!((t >> k) & 1)) ++k;
-  return k;
-}
-__host__ __device__ constexpr int gray_c(int t) { return t ^ (t >> 1); }
-
-template <class T> struct CtaRecord {
-  T min;
-  unsigned count;
-  unsigned ovf;
-  unsigned long long minstate;
-};
-
-struct Summary {
-  long long gmin;                 // minimum (quantised units for fixed64)
-  unsigned long long count;       // states at the minimum
-  unsigned ovf;                   // lists overflowed: collection pass needed
-  unsigned pad;
-  unsigned long long minstate;    // smallest state at the minimum
-  double energy;                  // FP64 energy (fixed64 path)
-  unsigned long long collected;   // collection pass: states written
-};
-
-template <class T> struct GrayParams {
-  T kf[INNER_MAX];                // inner step constants (kf[0] unused)
-  const T *q;                     // n x n symmetric coefficients
-  const T *kf_g;                  // global copy of kf (slow path)
-  int n;                          // row length (all variables)
-  int loop_bits;                  // blocks per item = 2^loop_bits
-  int item_bits;                  // number of items = 2^item_bits
-  int pad;
-  unsigned long long prefix_state;  // fixed top bits, in place
-  unsigned long long nstates;     // small kernel: states enumerated
-  unsigned long long *work;       // work-queue counter
-  long long *gbest;               // best energy found so far (pruning bound)
-  uint32_t seed;                  // descent starting points
-  unsigned long long fixed_mask;  // variables fixed by the shard prefix
-  unsigned long long var_mask;    // (1 << n) - 1
-  CtaRecord<T> *cta;              // one record per CTA
-  unsigned long long *cta_states; // CTA_CAP per CTA
-  // collection pass
-  const Summary *summary;         // gmin of the first pass
-  long long window;               // collect E <= gmin + window
-  unsigned long long *out_count;  // all states found
-  unsigned long long *out_pos;    // states written
-  unsigned long long *out_states;
-  unsigned long long out_cap;
-  unsigned long long *out_minstate;
-};
-
-template <class T> __device__ __forceinline__ T tmax();
-template <> __device__ __forceinline__ int tmax<int>() { return INT_MAX; }
-template <> __device__ __forceinline__ long long tmax<long long>() { return LLONG_MAX; }
-
-// One unrolled inner step; t, k and the direction are template constants.
-template <class T, int G, int t>
-__device__ __forceinline__ void inner_step(T &E, T &m, const T (&c)[G], const GrayParams<T> &P) {
-  constexpr int k = ctz_c(t);
-  constexpr bool up = (gray_c(t) >> k) & 1;
-  E += P.kf[t] + (up ? c[k] : -c[k]);
-  m = min(m, E);
-}
-
-template <class T, int G, int... Is>
-__device__ __forceinline__ void inner_block_impl(T &E, T &m, const T (&c)[G], const GrayParams<T> &P,
-                                                 std::integer_sequence<int, Is...>) {
-  (inner_step<T, G, Is + 1>(E, m, c, P), ...);
-}
-
-// The 2^G - 1 inner steps of one block, from inner state 0.
-template <class T, int G>
-__device__ __forceinline__ void inner_block(T &E, T &m, const T (&c)[G], const GrayParams<T> &P) {
-  inner_block_impl<T, G>(E, m, c, P, std::make_integer_sequence<int, (1 << G) - 1>{});
-}
-
-// Energy of a full state from scratch (set-bit pairs).
-template <class T>
-__device__ __forceinline__ T energy_from_scratch(const T *__restrict__ q, int n,
-                                                 unsigned long long x) {
-  T E = 0;
-  unsigned long long r = x;
-  while (r) {
-    int i = __ffsll((long long)r) - 1;
-    r &= r - 1;
-    const T *row = q + (size_t)i * n;
-    E += row[i];
-    unsigned long long r2 = r;
-    while (r2) {
-      int j = __ffsll((long long)r2) - 1;
-      r2 &= r2 - 1;
-      E += row[j];
-    }
-  }
-  return E;
-}
-
-template <class T> struct ThreadBest {
-  T best;
-  int cnt;
-  unsigned long long minstate;
-  unsigned long long list[LCAP];
-};
-
-// Inner couplings passed by value to the slow path, so that the hot loop's
-// copy never has its address taken and stays in registers.
-template <class T, int G> struct CVec {
-  T v[G];
-};
-
-struct CollectState {
-  unsigned long long count;
-  unsigned long long minstate;
-  bool full;
-};
-
-template <class T>
-__device__ __forceinline__ void note_state(ThreadBest<T> &tb, unsigned long long s, T e) {
-  if (e == tb.best) {
-    if (tb.cnt < LCAP) tb.list[tb.cnt] = s;
-    ++tb.cnt;
-    tb.minstate = min(tb.minstate, s);
-  }
-}
-
-template <class T>
-__device__ __forceinline__ void collect_state(CollectState &cs, const GrayParams<T> &P,
-                                              unsigned long long s, T e, T thr) {
-  if (e <= thr) {
-    ++cs.count;
-    cs.minstate = min(cs.minstate, s);
-    if (!cs.full) {
-      unsigned long long pos = atomicAdd(P.out_pos, 1ull);
-      if (pos < P.out_cap)
-        P.out_states[pos] = s;
-      else
-        cs.full = true;
-    }
-  }
-}
-
-// Greedy descent from a random state: repeatedly flip the single variable
-// that lowers the energy most, until none does. The energy reached is that
-// of a real state, so it is a valid upper bound on the minimum; it seeds the
-// per-thread pruning bound so that blocks are walked again only when they
-// reach the best energy known (a warp pays for the slow walk whenever any of
-// its lanes needs it).
-template <class T>
-__device__ __noinline__ T descent_bound(const GrayParams<T> &P, uint32_t tid) {
-  const int n = P.n;
-  const T *__restrict__ q = P.q;
-  const Philox4 r = philox4x32_10(tid, 0u, 0u, 0xE5000000u, P.seed, 0x9E3779B9u);
-  const unsigned long long rnd = ((unsigned long long)r.x << 32) | r.y;
-  unsigned long long x = P.prefix_state | (rnd & ~P.fixed_mask & P.var_mask);
-  T h[MAX_N];
-  for (int j = 0; j < n; ++j) {
-    T a = 0;
-    for (int i = 0; i < n; ++i)
-      if (i != j && ((x >> i) & 1ull)) a += q[(size_t)j * n + i];
-    h[j] = a;
-  }
-  T E = energy_from_scratch(q, n, x);
-  for (int it = 0; it < 4 * n; ++it) {
-    T best_d = 0;
-    int best_i = -1;
-    for (int i = 0; i < n; ++i) {
-      if ((P.fixed_mask >> i) & 1ull) continue;
-      const T loc = q[(size_t)i * n + i] + h[i];
-      const T d = ((x >> i) & 1ull) ? -loc : loc;
-      if (d < best_d) {
-        best_d = d;
-        best_i = i;
-      }
-    }
-    if (best_i < 0) break;
-    const bool was = (x >> best_i) & 1ull;
-    x ^= 1ull << best_i;
-    E += best_d;
-    for (int j = 0; j < n; ++j)
-      if (j != best_i) h[j] += was ? -q[(size_t)best_i * n + j] : q[(size_t)best_i * n + j];
-  }
-  return E;
-}
-
-// Slow path: walk one block again, state by state.
-template <class T, int G, bool COLLECT>
-__device__ __noinline__ void revisit_block(const GrayParams<T> &P, const CVec<T, G> c,
-                                           unsigned long long x_outer, T Estart, ThreadBest<T> &tb,
-                                           CollectState &cs, T thr) {
-  T e = Estart;
-  unsigned long long s = x_outer;
-  if (COLLECT) collect_state(cs, P, s, e, thr); else note_state(tb, s, e);
-  for (int t = 1; t < (1 << G); ++t) {
-    const int k = __ffs(t) - 1;
-    const bool up = ((t ^ (t >> 1)) >> k) & 1;
-    T ck = 0;
-#pragma unroll
-    for (int j = 0; j < G; ++j)
-      if (j == k) ck = c.v[j];
-    e += P.kf_g[t] + (up ? ck : -ck);
-    s ^= 1ull << k;
-    if (COLLECT) collect_state(cs, P, s, e, thr); else note_state(tb, s, e);
-  }
-}
-
-template <class T, int G, bool COLLECT>
-__device__ __forceinline__ void process_item(unsigned long long item, const GrayParams<T> &P,
-                                             ThreadBest<T> &tb, CollectState &cs, T thr) {
-  const int n = P.n;
-  const T *__restrict__ q = P.q;
-  unsigned long long x = P.prefix_state | (item << (G + P.loop_bits));
-  T E = energy_from_scratch(q, n, x);
-  T c[G];
-#pragma unroll
-  for (int i = 0; i < G; ++i) c[i] = 0;
-  {
-    unsigned long long r = x;
-    while (r) {
-      int j = __ffsll((long long)r) - 1;
-      r &= r - 1;
-      const T *row = q + (size_t)j * n;
-#pragma unroll
-      for (int i = 0; i < G; ++i) c[i] += row[i];
-    }
-  }
-  const T top_diag = q[(size_t)(G - 1) * n + (G - 1)];
-  const unsigned nblocks = 1u << P.loop_bits;
-  for (unsigned B = 0; B < nblocks; ++B) {
-    const T Estart = E;
-    T m = E;
-    inner_block<T, G>(E, m, c, P);
-    if (!COLLECT && (B & 7u) == 7u) {
-      // Tighten the bound with the best energy any thread has published.
-      const long long g = *reinterpret_cast<volatile long long *>(P.gbest);
-      if (g < (long long)tb.best) {
-        tb.best = (T)g;
-        tb.cnt = 0;
-        tb.minstate = ~0ull;
-      }
-    }
-    if (COLLECT ? (m <= thr) : (m <= tb.best)) {
-      if (!COLLECT && m < tb.best) {
-        tb.best = m;
-        tb.cnt = 0;
-        tb.minstate = ~0ull;
-        atomicMin(P.gbest, (long long)m);
-      }
-      CVec<T, G> cv;
-#pragma unroll
-      for (int i = 0; i < G; ++i) cv.v[i] = c[i];
-      revisit_block<T, G, COLLECT>(P, cv, x, Estart, tb, cs, thr);
-    }
-    if (B + 1 < nblocks) {
-      // Clear the top inner bit (the block ends at inner state 1 << (G-1)),
-      // then flip outer bit G + ctz(B+1) from inner state 0.
-      E -= top_diag + c[G - 1];
-      const int mb = G + __ffs((int)(B + 1)) - 1;
-      const unsigned long long bm = 1ull << mb;
-      const bool was = (x & bm) != 0;
-      const T *row = q + (size_t)mb * n;
-      T sum = row[mb];
-      unsigned long long r = x & ~bm;
-      while (r) {
-        int j = __ffsll((long long)r) - 1;
-        r &= r - 1;
-        sum += row[j];
-      }
-      E += was ? -sum : sum;
-      x ^= bm;
-#pragma unroll
-      for (int i = 0; i < G; ++i) c[i] += was ? -row[i] : row[i];
-    }
-  }
-}
-
-// CTA reduction of the per-thread bests into one record per CTA.
-template <class T>
-__device__ __forceinline__ void cta_reduce(const GrayParams<T> &P, ThreadBest<T> &tb) {
-  __shared__ T s_wmin[THREADS / 32];
-  __shared__ T s_min;
-  __shared__ unsigned s_count, s_ovf;
-  __shared__ unsigned long long s_minstate;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  T w = tb.cnt > 0 ? tb.best : tmax<T>();
-#pragma unroll
-  for (int off = 16; off > 0; off >>= 1) w = min(w, __shfl_xor_sync(0xffffffffu, w, off));
-  if (lane == 0) s_wmin[warp] = w;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    T mm = tmax<T>();
-    for (int i = 0; i < THREADS / 32; ++i) mm = min(mm, s_wmin[i]);
-    s_min = mm;
-    s_count = 0;
-    s_ovf = 0;
-    s_minstate = ~0ull;
-  }
-  __syncthreads();
-  const T cmin = s_min;
-  if (tb.cnt > 0 && tb.best == cmin) {
-    unsigned idx = atomicAdd(&s_count, (unsigned)tb.cnt);
-    if (tb.cnt > LCAP) atomicOr(&s_ovf, 1u);
-    atomicMin(&s_minstate, tb.minstate);
-    const int kept = min(tb.cnt, LCAP);
-    for (int e = 0; e < kept; ++e)
-      if (idx + e < CTA_CAP) P.cta_states[(size_t)blockIdx.x * CTA_CAP + idx + e] = tb.list[e];
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    CtaRecord<T> rec;
-    rec.min = cmin;
-    rec.count = s_count;
-    rec.ovf = (s_ovf || s_count > CTA_CAP) ? 1u : 0u;
-    rec.minstate = s_minstate;
-    P.cta[blockIdx.x] = rec;
-  }
-}
-
-template <class T, int G, bool COLLECT>
-__global__ void __launch_bounds__(THREADS) gray_kernel(const __grid_constant__ GrayParams<T> P) {
-  ThreadBest<T> tb;
-  tb.best = tmax<T>();
-  tb.cnt = 0;
-  tb.minstate = ~0ull;
-  CollectState cs{0ull, ~0ull, false};
-  T thr = 0;
-  if (COLLECT) {
-    thr = (T)(P.summary->gmin + P.window);
-  } else {
-    // Seed the pruning bound: one greedy descent per thread, reduced over
-    // the CTA and published to the global bound.
-    __shared__ long long s_bound;
-    if (threadIdx.x == 0) s_bound = LLONG_MAX;
-    __syncthreads();
-    const T d = descent_bound(P, blockIdx.x * blockDim.x + threadIdx.x);
-    atomicMin(&s_bound, (long long)d);
-    __syncthreads();
-    if (threadIdx.x == 0) atomicMin(P.gbest, s_bound);
-    const long long g = *reinterpret_cast<volatile long long *>(P.gbest);
-    tb.best = (T)min(s_bound, g);
-  }
-  const unsigned long long items = 1ull << P.item_bits;
-  const int lane = threadIdx.x & 31;
-  for (;;) {
-    unsigned long long base = 0;
-    if (lane == 0) base = atomicAdd(P.work, 32ull);
-    base = __shfl_sync(0xffffffffu, base, 0);
-    if (base >= items) break;
-    const unsigned long long item = base + lane;
-    if (item < items) process_item<T, G, COLLECT>(item, P, tb, cs, thr);
-  }
-  if (COLLECT) {
-    if (cs.count) {
-      atomicAdd(P.out_count, cs.count);
-      atomicMin(P.out_minstate, cs.minstate);
-    }
-  } else {
-    cta_reduce(P, tb);
-  }
-}
 
 // Few free bits: one thread per state, energies from scratch.
 template <class T, bool COLLECT>
@@ -555,6 +185,7 @@ struct os_exh_plan {
   int n = 0, fixed = 0, free_bits = 0;
   int kind = OS_COEF_INT32;
   int G = G_DEFAULT;             // unrolled inner bits
+  int variant = OS_EXH_VARIANT_ADD_MIN;
   bool small = false;
   unsigned long long prefix_state = 0;
   int ctas = 0;
@@ -606,7 +237,13 @@ void fill_params(os_exh_plan *p, GrayParams<T> &P, const std::vector<T> &q,
   OS_CUDA(cudaMemcpy(dq.get(), q.data(), sizeof(T) * q.size(), cudaMemcpyHostToDevice));
   dkf.alloc(INNER_MAX);
   OS_CUDA(cudaMemcpy(dkf.get(), kf.data(), sizeof(T) * INNER_MAX, cudaMemcpyHostToDevice));
-  for (int t = 0; t < INNER_MAX; ++t) P.kf[t] = kf[t];
+  T acc = 0;
+  for (int t = 0; t < INNER_MAX; ++t) {
+    P.kf[t] = kf[t];
+    acc += kf[t];
+    P.ks[t] = acc;
+  }
+  P.one = 1;
   P.q = dq.get();
   P.kf_g = dkf.get();
   P.n = n;
@@ -637,25 +274,19 @@ void fill_params(os_exh_plan *p, GrayParams<T> &P, const std::vector<T> &q,
   P.out_minstate = p->counters.get() + C_OUT_MIN;
 }
 
-// Launch gray_kernel<T, G, COLLECT> for a runtime G.
+// Launch gray_kernel for a runtime width G (9 or 10) and variant.
 template <class T, bool COLLECT>
-void launch_gray(int G, int grid, cudaStream_t s, const GrayParams<T> &P) {
-  switch (G) {
-    case 8: gray_kernel<T, 8, COLLECT><<<grid, THREADS, 0, s>>>(P); break;
-    case 9: gray_kernel<T, 9, COLLECT><<<grid, THREADS, 0, s>>>(P); break;
-    case 10: gray_kernel<T, 10, COLLECT><<<grid, THREADS, 0, s>>>(P); break;
-    default: throw_error(OS_INVALID_ARG, "inner_bits must be 8, 9 or 10");
-  }
+void launch_gray(int G, int variant, int grid, cudaStream_t s, const GrayParams<T> &P) {
+  if (G == 9)
+    launch_gray_width<T, 9>(variant, COLLECT, grid, s, P);
+  else if (G == 10)
+    launch_gray_width<T, 10>(variant, COLLECT, grid, s, P);
+  else
+    throw_error(OS_INVALID_ARG, "inner_bits must be 9 or 10");
 }
 
 template <class T> int gray_occupancy(int G) {
-  int occ = 0;
-  switch (G) {
-    case 8: OS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, gray_kernel<T, 8, false>, THREADS, 0)); break;
-    case 9: OS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, gray_kernel<T, 9, false>, THREADS, 0)); break;
-    default: OS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, gray_kernel<T, 10, false>, THREADS, 0)); break;
-  }
-  return occ < 1 ? 1 : occ;
+  return G == 9 ? gray_occupancy_width<T, 9>() : gray_occupancy_width<T, 10>();
 }
 
 template <class T> int grid_for(os_exh_plan *p, const GrayParams<T> &P) {
@@ -682,9 +313,9 @@ template <class T> void launch_pass(os_exh_plan *p, GrayParams<T> &P, bool colle
       small_kernel<T, false><<<p->ctas, THREADS, 0, s>>>(P);
   } else {
     if (collect)
-      launch_gray<T, true>(p->G, p->ctas, s, P);
+      launch_gray<T, true>(p->G, p->variant, p->ctas, s, P);
     else
-      launch_gray<T, false>(p->G, p->ctas, s, P);
+      launch_gray<T, false>(p->G, p->variant, p->ctas, s, P);
   }
   OS_CUDA(cudaGetLastError());
   ++p->launches;
@@ -769,8 +400,9 @@ os_status os_exhaustive_plan_create(os_ctx *ctx, const os_qubo_dense *qubo,
       else kind = OS_COEF_FIXED64;
     }
     OS_REQUIRE(kind >= OS_COEF_INT32 && kind <= OS_COEF_FIXED64, "unknown coef_kind %d", kind);
-    OS_REQUIRE(prm.inner_bits == 0 || (prm.inner_bits >= 8 && prm.inner_bits <= G_MAX),
-               "inner_bits must be 0 (default), 8, 9 or 10");
+    OS_REQUIRE(prm.inner_bits == 0 || prm.inner_bits == 9 || prm.inner_bits == 10,
+               "inner_bits must be 0 (default), 9 or 10");
+    OS_REQUIRE(prm.variant >= 0 && prm.variant <= OS_EXH_VARIANT_FUSED, "unknown variant %d", prm.variant);
     if (kind == OS_COEF_INT32)
       OS_REQUIRE(integral && abs_sum < 2147483000.0, "coefficients are not int32-exact");
     if (kind == OS_COEF_INT64)
@@ -785,6 +417,7 @@ os_status os_exhaustive_plan_create(os_ctx *ctx, const os_qubo_dense *qubo,
       p->kind = kind;
       p->small = p->free_bits < SMALL_FREE;
       p->G = prm.inner_bits ? prm.inner_bits : G_DEFAULT;
+      p->variant = prm.variant ? prm.variant : OS_EXH_VARIANT_DEFAULT;
       p->prefix_state = prm.fixed_high_bits ? (prm.prefix << p->free_bits) : 0ull;
       p->user_cap = prm.max_minimisers;
       p->out_cap = std::max<unsigned long long>(prm.max_minimisers, 1ull);
@@ -1018,7 +651,13 @@ void noalloc_run(const os_qubo_dense *qubo, const os_exh_params &prm, os_exh_res
   T kf[INNER_MAX];
   if (!small) inner_constants(q, n, G, kf);
   else for (int t = 0; t < INNER_MAX; ++t) kf[t] = 0;
-  for (int t = 0; t < INNER_MAX; ++t) P.kf[t] = kf[t];
+  T acc = 0;
+  for (int t = 0; t < INNER_MAX; ++t) {
+    P.kf[t] = kf[t];
+    acc += kf[t];
+    P.ks[t] = acc;
+  }
+  P.one = 1;
   unsigned long long *counters = reinterpret_cast<unsigned long long *>(base + NA_COUNTERS);
   Summary *summary = reinterpret_cast<Summary *>(base + NA_SUMMARY);
   T *dq = reinterpret_cast<T *>(base + NA_Q);
@@ -1054,7 +693,7 @@ void noalloc_run(const os_qubo_dense *qubo, const os_exh_params &prm, os_exh_res
     ctas = (int)ceil_div_u64(P.nstates, THREADS);
   } else {
     int occ = 0, sms = 0;
-    OS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, gray_kernel<T, G, false>, THREADS, 0));
+    occ = gray_occupancy_width<T, G>();
     OS_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
     const unsigned long long want = ceil_div_u64(1ull << P.item_bits, THREADS);
     ctas = (int)std::min<unsigned long long>(want, (unsigned long long)sms * std::max(occ, 1));
@@ -1071,7 +710,7 @@ void noalloc_run(const os_qubo_dense *qubo, const os_exh_params &prm, os_exh_res
   if (small) {
     small_kernel<T, false><<<ctas, THREADS, 0, s>>>(P);
   } else {
-    gray_kernel<T, G, false><<<ctas, THREADS, 0, s>>>(P);
+    launch_gray_width<T, G>(OS_EXH_VARIANT_ADD_MIN, false, ctas, s, P);
   }
   OS_CUDA(cudaGetLastError());
   gather_kernel<T><<<1, 1024, 0, s>>>(P.cta, ctas, P.cta_states, summary, P.out_states, P.out_cap);
@@ -1088,7 +727,7 @@ void noalloc_run(const os_qubo_dense *qubo, const os_exh_params &prm, os_exh_res
     if (small)
       small_kernel<T, true><<<ctas, THREADS, 0, s>>>(P);
     else
-      gray_kernel<T, G, true><<<ctas, THREADS, 0, s>>>(P);
+      launch_gray_width<T, G>(OS_EXH_VARIANT_ADD_MIN, true, ctas, s, P);
     OS_CUDA(cudaGetLastError());
     unsigned long long c3[3];
     OS_CUDA(cudaMemcpyAsync(c3, counters + C_OUT_COUNT, sizeof c3, cudaMemcpyDeviceToHost, s));

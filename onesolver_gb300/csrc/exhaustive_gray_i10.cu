@@ -1,0 +1,27 @@
+// Instances of the Gray-code enumeration kernel for int coefficients and
+// 10 inner bits, with their host-side launchers.
+#include "exhaustive_kernels.cuh"
+
+namespace os {
+namespace exh {
+
+template <>
+void launch_gray_width<int, 10>(int variant, bool collect, int grid, cudaStream_t s, const GrayParams<int> &P) {
+  if (collect)
+    gray_kernel<int, 10, true, 0><<<grid, THREADS, 0, s>>>(P);
+  else if (true && variant == OS_EXH_VARIANT_FUSED)
+    gray_kernel<int, 10, false, 1><<<grid, THREADS, 0, s>>>(P);
+  else
+    gray_kernel<int, 10, false, 0><<<grid, THREADS, 0, s>>>(P);
+  OS_CUDA(cudaGetLastError());
+}
+
+template <>
+int gray_occupancy_width<int, 10>() {
+  int occ = 0;
+  OS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, gray_kernel<int, 10, false, 0>, THREADS, 0));
+  return occ < 1 ? 1 : occ;
+}
+
+}  // namespace exh
+}  // namespace os

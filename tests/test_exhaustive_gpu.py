@@ -157,10 +157,11 @@ def test_n36_config(native, orc, ctx):
         assert part.energy >= res.energy
 
 
-@pytest.mark.parametrize("n", [14, 21, 27])
+@pytest.mark.parametrize("n", [14, 21, 27, 30])
 def test_inner_widths_agree(native, orc, ctx, n):
     f = random_int_qubo(n, 40 + n, -2, 2)
-    res = [native.exhaustive(f, ctx=ctx, inner_bits=g, max_minimisers=1 << 16) for g in (8, 9, 10)]
+    res = [native.exhaustive(f, ctx=ctx, inner_bits=g, variant=v, max_minimisers=1 << 16)
+           for g in (9, 10) for v in (1, 2)]
     for r in res[1:]:
         assert (r.energy, r.state, r.count, r.states.tolist()) == \
             (res[0].energy, res[0].state, res[0].count, res[0].states.tolist())
