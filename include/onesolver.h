@@ -288,6 +288,19 @@ typedef struct os_qubo_csr {
 os_status os_sa_run_sparse(os_ctx *ctx, const os_qubo_csr *qubo,
                            const os_sa_params *params, os_sa_result *result);
 
+/* Many independent dense instances (uneven n <= 1792) annealed with one
+ * shared schedule: every chunk of resync_every steps is one persistent
+ * work-queue launch over (instance, block of trajectories) items, largest
+ * instances first; the whole step sequence is captured once as a CUDA graph
+ * and replayed; the number of trajectories per CTA is picked by timing probe
+ * launches on the batch. num_tries trajectories per instance, sequential
+ * sweeps only, random initial spins. results[k] receives instance k's
+ * answer. No reference counterpart (the reference anneals one instance per
+ * sa::anneal call, annealing.hpp:55-140). */
+os_status os_sa_run_batched(os_ctx *ctx, int32_t num_instances,
+                            const os_qubo_dense *instances,
+                            const os_sa_params *params, os_sa_result *results);
+
 /* Deterministic verification mode. Runs the reference's Metropolis rule
  * (annealing.hpp:87-125) on the GPU with caller-given randoms in place of
  * oneMKL's philox4x32x10: init[t*n+i] replaces bit(), site[t*S+a] replaces
@@ -322,6 +335,14 @@ os_status os_sa_plan_create_dense(os_ctx *ctx, const os_qubo_dense *qubo,
                                   const os_sa_params *params, os_sa_plan **out);
 os_status os_sa_plan_create_sparse(os_ctx *ctx, const os_qubo_csr *qubo,
                                    const os_sa_params *params, os_sa_plan **out);
+/* Batched plan (see os_sa_run_batched); its answers come back through
+ * os_sa_plan_result_batched, one os_sa_result per instance. */
+os_status os_sa_plan_create_batched(os_ctx *ctx, int32_t num_instances,
+                                    const os_qubo_dense *instances,
+                                    const os_sa_params *params, os_sa_plan **out);
+os_status os_sa_plan_result_batched(os_sa_plan *plan, os_sa_result *results);
+/* Trajectories per CTA chosen by the batched plan's autotuner. */
+int32_t os_sa_plan_tuned_warps(const os_sa_plan *plan);
 os_status os_sa_plan_execute(os_sa_plan *plan);
 os_status os_sa_plan_result(os_sa_plan *plan, os_sa_result *result);
 int32_t os_sa_plan_launches(const os_sa_plan *plan);

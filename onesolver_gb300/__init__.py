@@ -135,6 +135,12 @@ SIGNATURES = {
     "os_sa_plan_result": (C.c_int, [_P, C.POINTER(_SaResult)]),
     "os_sa_plan_launches": (C.c_int32, [_P]),
     "os_sa_plan_destroy": (None, [_P]),
+    "os_sa_run_batched": (C.c_int, [_P, C.c_int32, C.POINTER(_QuboDense), C.POINTER(_SaParams),
+                                    C.POINTER(_SaResult)]),
+    "os_sa_plan_create_batched": (C.c_int, [_P, C.c_int32, C.POINTER(_QuboDense), C.POINTER(_SaParams),
+                                            C.POINTER(_P)]),
+    "os_sa_plan_result_batched": (C.c_int, [_P, C.POINTER(_SaResult)]),
+    "os_sa_plan_tuned_warps": (C.c_int32, [_P]),
     "os_sa_plan_kernel_ms": (C.c_int, [_P, C.POINTER(C.c_float)]),
     "os_philox_sample": (C.c_int, [_P, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.c_int32,
                                    C.POINTER(C.c_uint32)]),
@@ -588,6 +594,88 @@ class AnnealPlan:
         res, keep = _sa_result(self.n, self.T, traj_states)
         _check(lib().os_sa_plan_result(self._h, C.byref(res)))
         return _finish_sa(res, keep, self.n, self.T)
+
+    def close(self) -> None:
+        if self._h:
+            lib().os_sa_plan_destroy(self._h)
+            self._h = _P()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def _batch_inputs(instances):
+    fs = [np.ascontiguousarray(f, dtype=np.float64) for f in instances]
+    arr = (_QuboDense * len(fs))()
+    for k, f in enumerate(fs):
+        if f.ndim != 2 or f.shape[0] != f.shape[1]:
+            raise ValueError("QUBO matrices must be square")
+        arr[k] = _QuboDense(f.shape[0], _dptr(f))
+    return arr, fs
+
+
+def _batch_results(fs, T, traj_states):
+    res = (_SaResult * len(fs))()
+    keeps = []
+    for k, f in enumerate(fs):
+        r, keep = _sa_result(f.shape[0], T, traj_states)
+        res[k] = r
+        keeps.append(keep)
+    return res, keeps
+
+
+def anneal_batched(instances, beta: Sequence[float], *, num_tries: int = 256, sweeps_per_beta: int = 1,
+                   seed: int = 1234, acceptance: int = ACCEPT_PHYSICAL, resync_every: int = 0,
+                   ctx: Optional[Context] = None, traj_states: bool = False) -> list:
+    """Many dense instances (uneven n), one shared schedule, one persistent launch per chunk."""
+    ctx = ctx or default_context()
+    arr, fs = _batch_inputs(instances)
+    b = np.ascontiguousarray(beta, dtype=np.float64)
+    prm = _sa_params(b, sweeps_per_beta, num_tries, seed, acceptance, SITES_SEQUENTIAL, resync_every, None)
+    res, keeps = _batch_results(fs, num_tries, traj_states)
+    _check(lib().os_sa_run_batched(ctx.handle, len(fs), arr, C.byref(prm), res))
+    return [_finish_sa(res[k], keeps[k], fs[k].shape[0], num_tries) for k in range(len(fs))]
+
+
+class BatchedAnnealPlan:
+    """Device-resident batched anneal: create (autotunes) / execute (graph replay) / result."""
+
+    def __init__(self, instances, beta: Sequence[float], *, num_tries: int = 256, sweeps_per_beta: int = 1,
+                 seed: int = 1234, acceptance: int = ACCEPT_PHYSICAL, resync_every: int = 0,
+                 ctx: Optional[Context] = None):
+        self.ctx = ctx or default_context()
+        self.T = num_tries
+        self._arr, self._fs = _batch_inputs(instances)
+        self._b = np.ascontiguousarray(beta, dtype=np.float64)
+        prm = _sa_params(self._b, sweeps_per_beta, num_tries, seed, acceptance, SITES_SEQUENTIAL, resync_every,
+                         None)
+        self._h = _P()
+        _check(lib().os_sa_plan_create_batched(self.ctx.handle, len(self._fs), self._arr, C.byref(prm),
+                                               C.byref(self._h)))
+
+    def execute(self) -> None:
+        _check(lib().os_sa_plan_execute(self._h))
+
+    @property
+    def launches(self) -> int:
+        return int(lib().os_sa_plan_launches(self._h))
+
+    @property
+    def warps(self) -> int:
+        return int(lib().os_sa_plan_tuned_warps(self._h))
+
+    def kernel_ms(self) -> float:
+        v = C.c_float()
+        _check(lib().os_sa_plan_kernel_ms(self._h, C.byref(v)))
+        return float(v.value)
+
+    def result(self, traj_states: bool = False) -> list:
+        res, keeps = _batch_results(self._fs, self.T, traj_states)
+        _check(lib().os_sa_plan_result_batched(self._h, res))
+        return [_finish_sa(res[k], keeps[k], self._fs[k].shape[0], self.T) for k in range(len(self._fs))]
 
     def close(self) -> None:
         if self._h:

@@ -15,12 +15,17 @@
 #include "onesolver.h"
 #include "errors.hpp"
 
+// A failed runtime call also leaves its error in the thread's last-error
+// slot; clear it so that a later cudaGetLastError() check does not report a
+// stale failure.
 #define OS_CUDA(call)                                                          \
   do {                                                                         \
     cudaError_t err__ = (call);                                                \
-    if (err__ != cudaSuccess)                                                  \
+    if (err__ != cudaSuccess) {                                                \
+      (void)cudaGetLastError();                                                \
       ::os::throw_error(OS_CUDA_ERROR, "%s failed: %s (%s:%d)", #call,         \
                         cudaGetErrorString(err__), __FILE__, __LINE__);        \
+    }                                                                          \
   } while (0)
 
 namespace os {

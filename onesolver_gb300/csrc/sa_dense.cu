@@ -291,6 +291,7 @@ void os_sa_plan_common(os_sa_plan *p, os_ctx *ctx, const os_sa_params *prm, int 
 os_status os_sa_plan_result(os_sa_plan *p, os_sa_result *res) {
   return guard([&] {
     OS_REQUIRE(p && res, "null argument");
+    OS_REQUIRE(p->kind != 2, "batched plans return one result per instance (os_sa_plan_result_batched)");
     activate(p->ctx);
     cudaStream_t s = p->ctx->stream;
     OS_CUDA(cudaStreamSynchronize(s));
@@ -351,8 +352,10 @@ os_status os_sa_plan_execute(os_sa_plan *p) {
     activate(p->ctx);
     if (p->kind == 0)
       execute_dense(p);
-    else
+    else if (p->kind == 1)
       execute_sparse(p);
+    else
+      execute_batched(p);
   });
 }
 
@@ -377,6 +380,7 @@ void os_sa_plan_destroy(os_sa_plan *p) {
   if (!p) return;
   cudaSetDevice(p->ctx->device);
   cudaStreamSynchronize(p->ctx->stream);
+  release_batch(p);
   delete p;
 }
 

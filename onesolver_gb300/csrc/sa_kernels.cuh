@@ -31,6 +31,7 @@
 #include <cstdint>
 
 #include "philox.cuh"
+#include "rescore.cuh"
 #include "tma.cuh"
 
 namespace os {
@@ -217,14 +218,15 @@ __global__ void __launch_bounds__(128) sa_dense_rand_kernel(const __grid_constan
 constexpr int TILE_ROWS = 16;
 constexpr uint32_t TILE_WAIT_LIMIT = 1u << 26;
 
+// One item: the W trajectories of `a` (pointers already at the item's first
+// trajectory, warp w runs trajectory w), steps [step_begin, step_end).
+// `tiles` holds two buffers of TILE_ROWS x ld floats, `bar` their mbarriers,
+// `parity` their phase bits (kept by the caller across items). Returns false
+// when a bounded wait ran out (uniformly for the whole CTA).
 template <int SLOTS>
-__global__ void __launch_bounds__(256) sa_dense_tile_kernel(const __grid_constant__ DenseArgs a) {
-  extern __shared__ __align__(128) unsigned char tile_smem[];
-  __shared__ __align__(8) uint64_t bar[2];
-  float *tiles = reinterpret_cast<float *>(tile_smem);
+__device__ __forceinline__ bool tile_item(const DenseArgs &a, float *tiles, uint64_t *bar, uint32_t (&parity)[2]) {
   const int lane = threadIdx.x & 31;
-  const int W = blockDim.x >> 5;
-  const int t = blockIdx.x * W + (threadIdx.x >> 5);
+  const int t = threadIdx.x >> 5;
   const bool active = t < a.traj_count;
   const int nslots = a.nslots, ld = a.ld;
   const size_t tile_floats = (size_t)TILE_ROWS * ld;
@@ -251,12 +253,6 @@ __global__ void __launch_bounds__(256) sa_dense_tile_kernel(const __grid_constan
   const uint32_t tg = (uint32_t)(a.traj_offset + t);
   const uint32_t c3 = (a.instance & 0x0FFFFFFFu) | kStreamSweep;
 
-  if (threadIdx.x == 0) {
-    mbar_init(&bar[0], 1);
-    mbar_init(&bar[1], 1);
-    mbar_fence_init();
-  }
-  __syncthreads();
   auto issue = [&](long long g) {
     const int hs = (int)(g % halves);
     const int b = (int)(g & 1);
@@ -267,15 +263,13 @@ __global__ void __launch_bounds__(256) sa_dense_tile_kernel(const __grid_constan
     if (total > 0) issue(0);
     if (total > 1) issue(1);
   }
-  uint32_t parity[2] = {0u, 0u};
   long long g = 0;
-  bool failed = false;
-  for (int step = a.step_begin; step < a.step_end && !failed; ++step) {
+  for (int step = a.step_begin; step < a.step_end; ++step) {
     const float b = (float)a.beta[step / a.spb];
     Philox4 r{0, 0, 0, 0};
 #pragma unroll
     for (int s = 0; s < SLOTS; ++s) {
-      if (s >= nslots || failed) break;
+      if (s >= nslots) break;
       if ((s & 3) == 0)
         r = philox4x32_10((uint32_t)((s >> 2) * 32 + lane), (uint32_t)step, tg, c3, a.seed_lo, a.seed_hi);
       const float theta = threshold(select4(r, s & 3), b, a.acceptance);
@@ -316,22 +310,17 @@ __global__ void __launch_bounds__(256) sa_dense_tile_kernel(const __grid_constan
         }
         // Every warp is done with this buffer; refill it with tile g + 2.
         if (__syncthreads_or(!ok)) {
-          failed = true;
-          break;
+          // Let copies still in flight land (bounded) before returning.
+          if (threadIdx.x == 0) {
+            for (int b2 = 0; b2 < 2; ++b2) mbar_wait_bounded(&bar[b2], parity[b2], TILE_WAIT_LIMIT);
+            if (a.status) atomicExch(a.status, 1);
+          }
+          return false;
         }
         if (threadIdx.x == 0 && g + 2 < total) issue(g + 2);
         ++g;
       }
     }
-  }
-  if (failed) {
-    // Let copies still in flight land (bounded) before the CTA's shared
-    // memory is released, and report the timeout.
-    if (threadIdx.x == 0) {
-      for (int b2 = 0; b2 < 2; ++b2) mbar_wait_bounded(&bar[b2], parity[b2], TILE_WAIT_LIMIT);
-      if (a.status) atomicExch(a.status, 1);
-    }
-    return;
   }
   if (active) {
 #pragma unroll
@@ -344,6 +333,109 @@ __global__ void __launch_bounds__(256) sa_dense_tile_kernel(const __grid_constan
       a.ebest[t] = Eb;
       a.accepted[t] += acc;
     }
+  }
+  return true;
+}
+
+__device__ __forceinline__ void init_tile_barriers(uint64_t *bar) {
+  if (threadIdx.x == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    mbar_fence_init();
+  }
+  __syncthreads();
+}
+
+// One CTA per block of W trajectories of one instance.
+template <int SLOTS>
+__global__ void __launch_bounds__(512) sa_dense_tile_kernel(const __grid_constant__ DenseArgs a) {
+  extern __shared__ __align__(128) unsigned char tile_smem[];
+  __shared__ __align__(8) uint64_t bar[2];
+  init_tile_barriers(bar);
+  const int W = blockDim.x >> 5;
+  const size_t first = (size_t)blockIdx.x * W;
+  DenseArgs it = a;
+  it.traj_count = a.traj_count - (int)first < W ? a.traj_count - (int)first : W;
+  it.traj_offset = a.traj_offset + (int)first;
+  it.h = a.h + first * a.nslots * 32;
+  it.x = a.x + first * 32;
+  it.xbest = a.xbest + first * 32;
+  it.e = a.e + first;
+  it.ebest = a.ebest + first;
+  it.accepted = a.accepted + first;
+  uint32_t parity[2] = {0u, 0u};
+  tile_item<SLOTS>(it, reinterpret_cast<float *>(tile_smem), bar, parity);
+}
+
+// Many instances in one persistent launch: items are (instance, block of W
+// trajectories), taken largest first from a global counter.
+struct BatchInstance {
+  const float *c;
+  const float *diag;
+  const double *c64;
+  const double *d64;
+  const double *f;
+  int n, nslots, ld, T;
+  long long h_off;      // first field of the instance's first trajectory
+  long long traj_base;  // global index of its first trajectory
+};
+
+struct BatchArgs {
+  const BatchInstance *inst;
+  const int2 *items;           // (instance, first trajectory within it)
+  int num_items;
+  unsigned int *work;          // item counter
+  int W;
+  const double *beta;
+  int spb, step_begin, step_end, acceptance;
+  uint32_t seed_lo, seed_hi;
+  float *h;
+  unsigned long long *x, *xbest;
+  float *e, *ebest;
+  unsigned long long *accepted;
+  int *status;
+};
+
+template <int SLOTS>
+__global__ void __launch_bounds__(512) sa_batch_tile_kernel(const __grid_constant__ BatchArgs B) {
+  extern __shared__ __align__(128) unsigned char tile_smem[];
+  __shared__ __align__(8) uint64_t bar[2];
+  __shared__ int s_item;
+  init_tile_barriers(bar);
+  uint32_t parity[2] = {0u, 0u};
+  for (;;) {
+    if (threadIdx.x == 0) s_item = (int)atomicAdd(B.work, 1u);
+    __syncthreads();
+    const int item = s_item;
+    __syncthreads();
+    if (item >= B.num_items) break;
+    const int2 id = B.items[item];
+    const BatchInstance in = B.inst[id.x];
+    const long long g0 = in.traj_base + id.y;   // global trajectory index
+    DenseArgs a;
+    a.c = in.c;
+    a.diag = in.diag;
+    a.n = in.n;
+    a.nslots = in.nslots;
+    a.ld = in.ld;
+    a.spb = B.spb;
+    a.beta = B.beta;
+    a.step_begin = B.step_begin;
+    a.step_end = B.step_end;
+    a.acceptance = B.acceptance;
+    a.traj_count = in.T - id.y < B.W ? in.T - id.y : B.W;
+    a.traj_offset = id.y;
+    a.seed_lo = B.seed_lo;
+    a.seed_hi = B.seed_hi;
+    a.instance = (uint32_t)id.x;
+    a.h = B.h + in.h_off + (long long)id.y * in.nslots * 32;
+    a.x = B.x + g0 * 32;
+    a.xbest = B.xbest + g0 * 32;
+    a.e = B.e + g0;
+    a.ebest = B.ebest + g0;
+    a.accepted = B.accepted + g0;
+    a.status = B.status;
+    if (!tile_item<SLOTS>(a, reinterpret_cast<float *>(tile_smem), bar, parity)) break;
   }
 }
 
@@ -363,14 +455,13 @@ struct ResyncArgs {
   unsigned long long *drift_bits;  // max |h32 - h64| as ordered FP64 bits
 };
 
-// FP64 field resync (and initialisation): h_j = sum_{i set, i != j} Q_ij in
-// FP64 from the current spins, the drift of the FP32 fields against it, and
-// the FP64 energy E = sum_{i set} (Q_ii + h_i / 2).
+// FP64 field resync (and initialisation) of trajectory t of `a`:
+// h_j = sum_{i set, i != j} Q_ij in FP64 from the current spins, the drift of
+// the FP32 fields against it, and the FP64 energy E = sum_{i set} (Q_ii + h_i/2).
+// RNG index of the trajectory: a.traj_offset + t.
 template <int SLOTS>
-__global__ void __launch_bounds__(128) sa_dense_resync_kernel(const __grid_constant__ ResyncArgs a) {
+__device__ __forceinline__ void resync_traj(const ResyncArgs &a, int t) {
   const int lane = threadIdx.x & 31;
-  const int t = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  if (t >= a.traj_count) return;
   const int nslots = a.nslots;
   unsigned long long xl;
   if (a.init) {
@@ -431,8 +522,74 @@ __global__ void __launch_bounds__(128) sa_dense_resync_kernel(const __grid_const
   }
 }
 
+template <int SLOTS>
+__global__ void __launch_bounds__(128) sa_dense_resync_kernel(const __grid_constant__ ResyncArgs a) {
+  const int t = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (t >= a.traj_count) return;
+  resync_traj<SLOTS>(a, t);
+}
+
+// Batched resync: one warp per trajectory of any instance.
+struct BatchResyncArgs {
+  const BatchInstance *inst;
+  const int *traj_inst;        // instance of each global trajectory
+  long long total;
+  int init;
+  uint32_t seed_lo, seed_hi;
+  float *h;
+  unsigned long long *x, *xbest;
+  float *e, *ebest;
+  unsigned long long *drift_bits;
+};
+
+template <int SLOTS>
+__global__ void __launch_bounds__(128) sa_batch_resync_kernel(const __grid_constant__ BatchResyncArgs B) {
+  const long long gt = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (gt >= B.total) return;
+  const int k = B.traj_inst[gt];
+  const BatchInstance in = B.inst[k];
+  const int t = (int)(gt - in.traj_base);
+  ResyncArgs a;
+  a.c64 = in.c64;
+  a.d64 = in.d64;
+  a.n = in.n;
+  a.nslots = in.nslots;
+  a.ld = in.ld;
+  a.init = B.init;
+  a.init_prob = nullptr;
+  a.traj_count = in.T;
+  a.traj_offset = 0;
+  a.seed_lo = B.seed_lo;
+  a.seed_hi = B.seed_hi;
+  a.instance = (uint32_t)k;
+  a.h = B.h + in.h_off;
+  a.x = B.x + in.traj_base * 32;
+  a.xbest = B.xbest + in.traj_base * 32;
+  a.e = B.e + in.traj_base;
+  a.ebest = B.ebest + in.traj_base;
+  a.drift_bits = B.drift_bits;
+  resync_traj<SLOTS>(a, t);
+}
+
+// Batched best states -> bytes and FP64 re-score in the reference's order
+// (one warp per trajectory; lane 0 adds the set pairs in row-major order).
+static __global__ void sa_batch_rescore_kernel(const BatchInstance *__restrict__ inst, const int *__restrict__ traj_inst,
+                                        const long long *__restrict__ state_off, long long total,
+                                        const unsigned long long *__restrict__ xbest, uint8_t *__restrict__ states,
+                                        double *__restrict__ e64) {
+  const long long gt = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (gt >= total) return;
+  const BatchInstance in = inst[traj_inst[gt]];
+  uint8_t *out = states + state_off[gt];
+  for (int site = lane; site < in.n; site += 32)
+    out[site] = (uint8_t)((xbest[gt * 32 + (site & 31)] >> (site >> 5)) & 1ull);
+  __syncwarp();
+  if (lane == 0) e64[gt] = rescore_energy(in.f, in.n, out);
+}
+
 // Best states as one byte per variable, for the FP64 re-score.
-__global__ void unpack_states_kernel(const unsigned long long *__restrict__ xbest, int n,
+static __global__ void unpack_states_kernel(const unsigned long long *__restrict__ xbest, int n,
                                      int traj_count, uint8_t *__restrict__ out) {
   const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= (size_t)traj_count * n) return;

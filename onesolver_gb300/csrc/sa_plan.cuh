@@ -6,9 +6,16 @@
 
 #include "common.cuh"
 
+namespace os {
+namespace sa {
+struct BatchState;
+}  // namespace sa
+}  // namespace os
+
 struct os_sa_plan {
   os_ctx *ctx = nullptr;
-  int kind = 0;                 // 0 dense, 1 sparse
+  int kind = 0;                 // 0 dense, 1 sparse, 2 batched dense
+  os::sa::BatchState *batch = nullptr;
   int n = 0, T = 0;
   int spb = 1, num_iter = 0, steps = 0, chunk = 0;
   unsigned long long seed = 0;
@@ -68,6 +75,8 @@ namespace os {
 namespace sa {
 void execute_dense(os_sa_plan *p);
 void execute_sparse(os_sa_plan *p);
+void execute_batched(os_sa_plan *p);
+void release_batch(os_sa_plan *p);
 }  // namespace sa
 }  // namespace os
 

@@ -243,3 +243,53 @@ def test_sparse_rejects_bad_csr(native, ctx):
     bad.val[0] += 1.0  # breaks symmetry
     with pytest.raises(native.OneSolverError):
         native.anneal_sparse(bad, [1.0], ctx=ctx)
+
+
+# ---------------------------------------------------------------------------
+# Batched (many instances, one persistent launch per chunk, CUDA graph)
+# ---------------------------------------------------------------------------
+
+def _batch_instances():
+    sizes = (40, 64, 100, 130, 33, 257)
+    return [random_normal_qubo(n, 100 + n, scale=1.0 / np.sqrt(n)) for n in sizes]
+
+
+def test_batched_rescore_and_statistics(native, orc, ctx):
+    fs = _batch_instances()
+    beta = native.geometric_schedule(0.1, 5.0, 40)
+    rs = native.anneal_batched(fs, beta, num_tries=160, resync_every=16, ctx=ctx, traj_states=True)
+    assert len(rs) == len(fs)
+    for f, r in zip(fs, rs):
+        _rescore_ok(orc, f, r)
+        assert r.attempts == 160 * 40 * f.shape[0]
+        assert r.max_field_drift < 1e-4
+        single = native.anneal(f, beta, num_tries=160, site_order=1, acceptance=1, resync_every=16, seed=77,
+                               ctx=ctx)
+        ks = stats.ks_2samp(r.traj_energies, single.traj_energies)
+        assert ks.pvalue > 1e-3, (f.shape[0], ks)
+
+
+def test_batched_plan_graph_replay_and_autotune(native, orc, ctx):
+    fs = _batch_instances()[:4]
+    beta = native.geometric_schedule(0.1, 3.0, 24)
+    plan = native.BatchedAnnealPlan(fs, beta, num_tries=64, resync_every=8, ctx=ctx)
+    assert plan.warps in (4, 8, 16)
+    plan.execute()
+    r1 = plan.result(traj_states=True)
+    plan.execute()  # replays the captured graph
+    r2 = plan.result(traj_states=True)
+    for a, b, f in zip(r1, r2, fs):
+        assert np.array_equal(a.traj_energies, b.traj_energies)
+        assert np.array_equal(a.traj_states, b.traj_states)
+        _rescore_ok(orc, f, a)
+    assert plan.kernel_ms() > 0
+    plan.close()
+
+
+def test_batched_rejects_random_order(native, ctx):
+    with pytest.raises(native.OneSolverError):
+        arr, fs = native._batch_inputs(_batch_instances()[:2])
+        b = np.ascontiguousarray([1.0])
+        prm = native._sa_params(b, 1, 8, 1, 1, native.SITES_RANDOM, 0, None)
+        res, keeps = native._batch_results(fs, 8, False)
+        native._check(native.lib().os_sa_run_batched(ctx.handle, len(fs), arr, native.C.byref(prm), res))
