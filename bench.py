@@ -17,6 +17,12 @@ Workloads (--workload):
                 N(0, 1/n); 256 trajectories x 2,000 sweeps each, geometric
                 beta 0.1 -> 5.0, one persistent launch per 250-sweep chunk,
                 CUDA-graph replay, autotuned trajectories per CTA.
+  sa-learned    Learned warm start on SK n = 1024 (J_ij ~ N(0, 1/n)): labels from
+                plain batched SA on --learned-train seeded training instances,
+                the message-passing net trained on the GPU, then on
+                --learned-eval held-out seeds the time-to-target (within 0.5%
+                of a long plain-SA best) of the gated warm start vs plain
+                random-init SA, 512 trajectories each. Metric: seconds.
   sa-n64        Dense SA, n = 64, N(0,1) entries (seed 0), 100 trajectories x
                 100 random-site steps, geometric beta 0.1 -> 1.0 with the
                 reference's acceptance rule. Metric: spin-flip attempts/s.
@@ -418,6 +424,60 @@ def bench_sa(args, ctx, pg, rank, world, workload):
     return out
 
 
+def bench_learned(args, ctx, pg, rank, world):
+    import torch
+    import onesolver_gb300 as osg
+    from onesolver_gb300 import warmstart as ws
+    n = 1024
+    t0 = time.perf_counter()
+    train = [ws.sk_qubo(n, s) for s in range(args.learned_train)]
+    labels = ws.label_states(train, num_tries=64, sweeps=500, ctx=ctx)
+    t_label = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    net, hist = ws.train_net(train, labels, epochs=args.learned_epochs, lr=2e-3, ctx=ctx)
+    t_train = time.perf_counter() - t0
+    del train
+    rows = []
+    for k in range(args.learned_eval):
+        f = ws.sk_qubo(n, 10000 + k)
+        target = osg.anneal(f, osg.geometric_schedule(0.1, 5.0, args.learned_target_sweeps), num_tries=512,
+                            site_order=1, acceptance=osg.ACCEPT_PHYSICAL, resync_every=500, seed=99,
+                            ctx=ctx).energy
+        prob = net.predict(f)
+        gate = ws.probe_gate(f, prob, ctx=ctx)
+        cold = ws.time_to_target(f, target, ctx=ctx)
+        warm = ws.time_to_target(f, target, init_prob=prob, beta_min=1.0, ctx=ctx)
+        chosen = warm if gate.use_warm else cold
+        rows.append({"seed": 10000 + k, "target": target, "use_warm": gate.use_warm,
+                     "probe_warm": gate.warm_energy, "probe_cold": gate.cold_energy,
+                     "plain_sweeps": cold.sweeps, "plain_s": cold.seconds,
+                     "warm_sweeps": warm.sweeps, "warm_s": warm.seconds,
+                     "chosen_s": chosen.seconds})
+    def med(key):
+        v = [r[key] for r in rows if r[key] is not None]
+        return statistics.median(v) if v else None
+    succ = lambda key: sum(r[key] is not None for r in rows) / len(rows)
+    value = med("chosen_s")
+    out = {
+        "metric": "SA time-to-target (within 0.5% of a long plain-SA best), learned warm start with probe gate",
+        "value": value, "unit": "s", "ms_per_step": None, "dtype": "fp32 fields, bf16 network",
+        "higher_is_better": False,
+        "config": {"workload": f"SK n=1024 J~N(0,1/n); {args.learned_train} training instances (labels: plain "
+                               f"batched SA 64 traj x 500 sweeps); {args.learned_eval} held-out seeds; target = "
+                               f"best of plain SA 512 traj x {args.learned_target_sweeps} sweeps; 512 trajectories "
+                               "per time-to-target run; warm runs start at beta 1.0, plain at 0.1 (geometric to 5.0)",
+                   "network": "3 message-passing layers, hidden 64, BF16 mma.sync + FP32"},
+        "result": {"plain_median_s": med("plain_s"), "warm_median_s": med("warm_s"),
+                   "plain_success": succ("plain_s"), "warm_success": succ("warm_s"),
+                   "gate_uses_warm": sum(r["use_warm"] for r in rows), "instances": rows,
+                   "train_loss_first_last": [float(hist[0]), float(hist[-1])] if len(hist) else None,
+                   "label_s": t_label, "train_s": t_train},
+        "gpu_launches": None,
+    }
+    net.close()
+    return out
+
+
 # DRAM bytes per launch of the dominant kernel, from the ncu captures
 # summarised under profiles/ (null until captured).
 TRAFFIC: dict = {}
@@ -510,6 +570,7 @@ METRICS = {
     "sa-sk": "SA spin-flip attempts/s",
     "sa-batch": "SA spin-flip attempts/s",
     "sa-n64": "SA spin-flip attempts/s",
+    "sa-learned": "SA time-to-target, learned warm start vs plain",
 }
 CONFIG_NAMES = {
     "exhaustive36": "exhaustive search, dense QUBO n=36, integer Q_ij ~ U{-8..8} (seed 0), 2^36 states",
@@ -517,6 +578,7 @@ CONFIG_NAMES = {
     "sa-sk": "dense SA, SK n=1024, 512 trajectories x 1,000 sweeps",
     "sa-batch": "batched dense SA, 512 instances n~U[64,1024], 256 trajectories x 2,000 sweeps",
     "sa-n64": "dense SA, n=64, 100 trajectories x 100 steps (reference CLI defaults)",
+    "sa-learned": "SK n=1024 learned warm start, time-to-target",
 }
 
 
@@ -531,9 +593,14 @@ def main():
                     help="also measure the SA workloads and report them under 'secondary'")
     ap.add_argument("--cpu-baseline", action=argparse.BooleanOptionalAction, default=True)
     ap.add_argument("--ref-budget", type=float, default=8.0, help="seconds of CPU work per reference step")
+    ap.add_argument("--learned-train", type=int, default=256)
+    ap.add_argument("--learned-eval", type=int, default=8)
+    ap.add_argument("--learned-epochs", type=int, default=20)
+    ap.add_argument("--learned-target-sweeps", type=int, default=4000)
     args = ap.parse_args()
     if args.steps <= 0:
-        args.steps = {"exhaustive36": 50, "sa-chimera": 10, "sa-sk": 5, "sa-batch": 3, "sa-n64": 50}[args.workload]
+        args.steps = {"exhaustive36": 50, "sa-chimera": 10, "sa-sk": 5, "sa-batch": 3, "sa-n64": 50,
+                      "sa-learned": 1}[args.workload]
     args.warmup = max(args.warmup, 3)
 
     world, rank, local, pg = dist_setup(args.gpus)
@@ -556,6 +623,8 @@ def main():
 
     if args.workload == "exhaustive36":
         out = bench_exhaustive(args, ctx, pg, rank, world)
+    elif args.workload == "sa-learned":
+        out = bench_learned(args, ctx, pg, rank, world)
     else:
         out = bench_sa(args, ctx, pg, rank, world, args.workload)
 
@@ -571,7 +640,7 @@ def main():
                       "e2e": r["e2e"]["value"], "result": r["result"], "gpu_launches": r["gpu_launches"]}
         out["secondary"] = sec
 
-    if rank == 0 and world == 1 and args.cpu_baseline:
+    if rank == 0 and world == 1 and args.cpu_baseline and args.workload != "sa-learned":
         threads = os.cpu_count() or 1
         if args.workload == "exhaustive36":
             rate, sample, dt = cpu_exhaustive_rate(int_qubo(36, 0), 15.0, threads)
@@ -586,7 +655,7 @@ def main():
     if rank == 0:
         line = {"metric": out["metric"], "value": out["value"], "unit": out["unit"], "n_gpus": world,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": out["ms_per_step"],
-                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": out["dtype"],
+                "higher_is_better": out.get("higher_is_better", True), "scaling": "weak", "vs_baseline": None, "dtype": out["dtype"],
                 "data": "synthetic (seeded; shapes and distributions of the configs)", "config": out["config"]}
         for k in ("roofline", "cpu_baseline", "e2e", "gpu_launches", "clocks", "result", "secondary"):
             if k in out:

@@ -359,6 +359,37 @@ os_status os_philox_sample(os_ctx *ctx, const uint32_t ctr[4],
                            const uint32_t key[2], int32_t count,
                            uint32_t *out);
 
+/* ------------------------------------------------------------------------ */
+/* Learned warm start (no reference counterpart)                            */
+/* ------------------------------------------------------------------------ */
+
+/* A message-passing network over the coupling matrix that predicts per-spin
+ * probabilities P(x_i = 1) for os_sa_params.init_prob. The reference always
+ * starts from fair coins (annealing.hpp:91-93); plain random-init annealing
+ * stays the fallback. Hidden width 64 (the kernels are built for it), 1..8
+ * layers; BF16 tensor-core (mma.sync) products with FP32 accumulation for
+ * the coupling-matrix messages, FP32 elsewhere; Adam on the GPU. With
+ * orient = 1 labels are oriented so that spin 0 is 1 and predictions come
+ * in that orientation (for field-free Ising QUBOs, which are symmetric under
+ * the global flip); orient = 0 keeps labels as given. */
+typedef struct os_mpnn os_mpnn;
+os_status os_mpnn_create(os_ctx *ctx, int32_t hidden, int32_t layers, int32_t orient, uint64_t seed,
+                         os_mpnn **out);
+void os_mpnn_destroy(os_mpnn *model);
+int64_t os_mpnn_num_params(const os_mpnn *model);
+os_status os_mpnn_get_params(os_mpnn *model, float *out, size_t cap);
+os_status os_mpnn_set_params(os_mpnn *model, const float *in, size_t count);
+/* Stage an instance (and optionally its label state, n chars) on the GPU. */
+os_status os_mpnn_add_instance(os_mpnn *model, const os_qubo_dense *qubo, const char *label, int32_t *index);
+os_status os_mpnn_clear_instances(os_mpnn *model);
+/* Mean BCE loss and its gradient (os_mpnn_num_params floats) for one stored
+ * labelled instance at the current parameters. */
+os_status os_mpnn_loss_grad(os_mpnn *model, int32_t index, float *loss, float *grads, size_t cap);
+/* `epochs` passes of Adam (one step per labelled instance, shuffled). */
+os_status os_mpnn_train(os_mpnn *model, int32_t epochs, float lr, uint64_t shuffle_seed, float *epoch_loss);
+/* Per-spin P(x_i = 1) (n floats) for a new instance. */
+os_status os_mpnn_predict(os_mpnn *model, const os_qubo_dense *qubo, float *prob);
+
 /* Measured roofline denominators for the two integer/FP32-bound paths (the
  * measured peaks cover HBM copy bandwidth and bf16 GEMMs only): the
  * INT32 issue rate of the enumeration's per-state instruction pair (three-

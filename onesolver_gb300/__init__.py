@@ -144,6 +144,16 @@ SIGNATURES = {
     "os_sa_plan_kernel_ms": (C.c_int, [_P, C.POINTER(C.c_float)]),
     "os_philox_sample": (C.c_int, [_P, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.c_int32,
                                    C.POINTER(C.c_uint32)]),
+    "os_mpnn_create": (C.c_int, [_P, C.c_int32, C.c_int32, C.c_int32, C.c_uint64, C.POINTER(_P)]),
+    "os_mpnn_destroy": (None, [_P]),
+    "os_mpnn_num_params": (C.c_int64, [_P]),
+    "os_mpnn_get_params": (C.c_int, [_P, C.POINTER(C.c_float), C.c_size_t]),
+    "os_mpnn_set_params": (C.c_int, [_P, C.POINTER(C.c_float), C.c_size_t]),
+    "os_mpnn_add_instance": (C.c_int, [_P, C.POINTER(_QuboDense), C.c_char_p, C.POINTER(C.c_int32)]),
+    "os_mpnn_clear_instances": (C.c_int, [_P]),
+    "os_mpnn_loss_grad": (C.c_int, [_P, C.c_int32, C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_size_t]),
+    "os_mpnn_train": (C.c_int, [_P, C.c_int32, C.c_float, C.c_uint64, C.POINTER(C.c_float)]),
+    "os_mpnn_predict": (C.c_int, [_P, C.POINTER(_QuboDense), C.POINTER(C.c_float)]),
     "os_probe_int32_peak": (C.c_int, [_P, C.POINTER(C.c_double)]),
     "os_probe_fp32_fma_peak": (C.c_int, [_P, C.POINTER(C.c_double)]),
 }
@@ -733,6 +743,71 @@ def energy_batch(f: np.ndarray, states: np.ndarray, *, ctx: Optional[Context] = 
     out = np.zeros(m)
     _check(lib().os_energy_batch(ctx.handle, C.byref(q), s.ctypes.data_as(C.c_char_p), m, _dptr(out)))
     return out
+
+
+class WarmStartNet:
+    """The learned warm start: message-passing network trained on the GPU.
+
+    ``add(f, label)`` stages a training instance (label: the best state found,
+    n 0/1 values), ``train(epochs, lr)`` runs Adam, ``predict(f)`` returns
+    per-spin P(x_i = 1) for ``anneal(..., init_prob=...)``.
+    """
+
+    def __init__(self, *, hidden: int = 64, layers: int = 3, orient: bool = True, seed: int = 1,
+                 ctx: Optional[Context] = None):
+        self.ctx = ctx or default_context()
+        self._h = _P()
+        self.orient = orient
+        _check(lib().os_mpnn_create(self.ctx.handle, hidden, layers, int(orient), seed, C.byref(self._h)))
+        self.num_params = int(lib().os_mpnn_num_params(self._h))
+        self._keep = []
+
+    def params(self) -> np.ndarray:
+        out = np.zeros(self.num_params, dtype=np.float32)
+        _check(lib().os_mpnn_get_params(self._h, out.ctypes.data_as(C.POINTER(C.c_float)), out.size))
+        return out
+
+    def set_params(self, p: np.ndarray) -> None:
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        _check(lib().os_mpnn_set_params(self._h, p.ctypes.data_as(C.POINTER(C.c_float)), p.size))
+
+    def add(self, f: np.ndarray, label=None) -> int:
+        q, keep = _dense(f)
+        lab = None if label is None else bytes(bytearray(int(v) for v in label))
+        idx = C.c_int32(-1)
+        _check(lib().os_mpnn_add_instance(self._h, C.byref(q), lab, C.byref(idx)))
+        return idx.value
+
+    def clear(self) -> None:
+        _check(lib().os_mpnn_clear_instances(self._h))
+
+    def loss_grad(self, index: int):
+        loss = C.c_float()
+        g = np.zeros(self.num_params, dtype=np.float32)
+        _check(lib().os_mpnn_loss_grad(self._h, index, C.byref(loss), g.ctypes.data_as(C.POINTER(C.c_float)), g.size))
+        return float(loss.value), g
+
+    def train(self, epochs: int, lr: float = 1e-3, seed: int = 0) -> np.ndarray:
+        out = np.zeros(max(epochs, 1), dtype=np.float32)
+        _check(lib().os_mpnn_train(self._h, epochs, lr, seed, out.ctypes.data_as(C.POINTER(C.c_float))))
+        return out[:epochs]
+
+    def predict(self, f: np.ndarray) -> np.ndarray:
+        q, keep = _dense(f)
+        out = np.zeros(q.n, dtype=np.float32)
+        _check(lib().os_mpnn_predict(self._h, C.byref(q), out.ctypes.data_as(C.POINTER(C.c_float))))
+        return out
+
+    def close(self) -> None:
+        if self._h:
+            lib().os_mpnn_destroy(self._h)
+            self._h = _P()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def probe_int32_peak(ctx: Optional[Context] = None) -> float:

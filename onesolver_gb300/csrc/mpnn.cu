@@ -1,0 +1,590 @@
+// mpnn.cu -- the learned warm start: a small message-passing network over the
+// coupling matrix that predicts per-spin probabilities P(x_i = 1), trained
+// on the GPU by the library's own forward, backward and Adam kernels.
+//
+// No reference counterpart: the reference always starts trajectories from
+// fair coins (include/simulated_annealing/annealing.hpp:91-93). Its output
+// feeds os_sa_params.init_prob; plain random-init annealing stays the
+// fallback and the judge of the energy gap.
+//
+// Network (H hidden units, L message-passing layers, n spins):
+//   C^      = C / (rms(C) sqrt(n))           off-diagonal couplings, BF16
+//   X       = [1, d_i / s, r_i / s, [i == 0]] node features: diagonal d_i,
+//             row sum r_i of C, scale s = rms(C) sqrt(n); spin 0 is the anchor
+//   H0      = relu(X W_in + b_in)
+//   M_l     = C^ H_{l-1}                      (n x n) x (n x H) BF16 tensor cores
+//   H_l     = relu(H_{l-1} Ws_l + M_l Wm_l + b_l),   l = 1..L
+//   logit   = H_L w_out + b_out,  p = sigmoid(logit)
+//   loss    = mean BCE(p_i, y_i)
+// A QUBO from a field-free Ising model has the global flip symmetry
+// E(x) = E(1 - x) + const; for such instances labels are oriented with
+// y_0 = 1 (the anchor feature tells the network which spin that is) and the
+// prediction is in that orientation. General QUBOs keep their labels as given.
+//
+// The (n x n) x (n x H) products run on the tensor cores with mma.sync
+// m16n8k16 BF16 -> FP32; the small (n x H) x (H x H) products, the weight
+// gradients and the element-wise parts run on FP32 CUDA cores.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <vector>
+
+#include <cuda_bf16.h>
+
+#include "common.cuh"
+#include "philox.cuh"
+
+namespace os {
+namespace mpnn {
+
+constexpr int FEAT = 4;
+
+// ---------------------------------------------------------------------------
+// C^ (n x n, BF16, row-major) times Hb (n x H, BF16, row-major) -> out
+// (n x H, FP32). CTA: 64 rows x 64 columns, 4 warps of 16 rows, K step 32.
+// ---------------------------------------------------------------------------
+constexpr int GM = 64, GN = 64, GK = 32;
+
+__device__ __forceinline__ void mma_bf16_16816(float (&d)[4], const uint32_t (&a)[4], const uint32_t (&b)[2]) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+      "{%0,%1,%2,%3};\n"
+      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
+__device__ __forceinline__ uint32_t pack2(__nv_bfloat16 lo, __nv_bfloat16 hi) {
+  uint32_t r;
+  r = (uint32_t)__bfloat16_as_ushort(lo) | ((uint32_t)__bfloat16_as_ushort(hi) << 16);
+  return r;
+}
+
+// Requires n % 32 == 0 (padded) and H == 64.
+__global__ void __launch_bounds__(128) gemm_ch_kernel(const __nv_bfloat16 *__restrict__ A, int n,
+                                                      const __nv_bfloat16 *__restrict__ B, float *__restrict__ out) {
+  __shared__ __nv_bfloat16 sA[GM][GK + 8];
+  __shared__ __nv_bfloat16 sB[GK][GN + 8];
+  const int row0 = blockIdx.x * GM;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int g = lane >> 2, tg = lane & 3;
+  float acc[GN / 8][4];
+#pragma unroll
+  for (int j = 0; j < GN / 8; ++j)
+#pragma unroll
+    for (int e = 0; e < 4; ++e) acc[j][e] = 0.f;
+  for (int k0 = 0; k0 < n; k0 += GK) {
+    // Stage A (64 x 32) and B (32 x 64): 2048 elements each, 16 per thread.
+    for (int i = threadIdx.x; i < GM * GK; i += blockDim.x) {
+      const int r = i / GK, c = i % GK;
+      const int gr = row0 + r;
+      sA[r][c] = gr < n ? A[(size_t)gr * n + k0 + c] : __float2bfloat16(0.f);
+    }
+    for (int i = threadIdx.x; i < GK * GN; i += blockDim.x) {
+      const int r = i / GN, c = i % GN;
+      sB[r][c] = B[(size_t)(k0 + r) * GN + c];
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < GK; kk += 16) {
+      uint32_t a[4];
+      const int ar = warp * 16 + g;
+      a[0] = pack2(sA[ar][kk + tg * 2], sA[ar][kk + tg * 2 + 1]);
+      a[1] = pack2(sA[ar + 8][kk + tg * 2], sA[ar + 8][kk + tg * 2 + 1]);
+      a[2] = pack2(sA[ar][kk + tg * 2 + 8], sA[ar][kk + tg * 2 + 9]);
+      a[3] = pack2(sA[ar + 8][kk + tg * 2 + 8], sA[ar + 8][kk + tg * 2 + 9]);
+#pragma unroll
+      for (int j = 0; j < GN / 8; ++j) {
+        uint32_t b[2];
+        const int bc = j * 8 + g;
+        b[0] = pack2(sB[kk + tg * 2][bc], sB[kk + tg * 2 + 1][bc]);
+        b[1] = pack2(sB[kk + tg * 2 + 8][bc], sB[kk + tg * 2 + 9][bc]);
+        mma_bf16_16816(acc[j], a, b);
+      }
+    }
+    __syncthreads();
+  }
+  const int r_lo = row0 + warp * 16 + g, r_hi = r_lo + 8;
+#pragma unroll
+  for (int j = 0; j < GN / 8; ++j) {
+    const int c = j * 8 + tg * 2;
+    if (r_lo < n) {
+      out[(size_t)r_lo * GN + c] = acc[j][0];
+      out[(size_t)r_lo * GN + c + 1] = acc[j][1];
+    }
+    if (r_hi < n) {
+      out[(size_t)r_hi * GN + c] = acc[j][2];
+      out[(size_t)r_hi * GN + c + 1] = acc[j][3];
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Small FP32 kernels
+// ---------------------------------------------------------------------------
+
+// out[n x Hh] = A[n x K] W[K x Hh] (+ B[n x K] W2[K x Hh]) (+ bias), optional relu.
+__global__ void linear_kernel(const float *__restrict__ A, const float *__restrict__ W, const float *__restrict__ B,
+                              const float *__restrict__ W2, const float *__restrict__ bias, int n, int K, int Hh,
+                              int relu, float *__restrict__ pre, float *__restrict__ out) {
+  const int i = blockIdx.x;
+  const int h = threadIdx.x;
+  if (i >= n || h >= Hh) return;
+  float acc = bias ? bias[h] : 0.f;
+  for (int k = 0; k < K; ++k) acc = fmaf(A[(size_t)i * K + k], W[(size_t)k * Hh + h], acc);
+  if (B)
+    for (int k = 0; k < K; ++k) acc = fmaf(B[(size_t)i * K + k], W2[(size_t)k * Hh + h], acc);
+  if (pre) pre[(size_t)i * Hh + h] = acc;
+  out[(size_t)i * Hh + h] = relu ? fmaxf(acc, 0.f) : acc;
+}
+
+__global__ void to_bf16_kernel(const float *__restrict__ in, __nv_bfloat16 *__restrict__ out, size_t count) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < count) out[i] = __float2bfloat16(in[i]);
+}
+
+// logits, probabilities, loss terms and dlogit for one instance.
+__global__ void head_kernel(const float *__restrict__ Hl, const float *__restrict__ w, const float *__restrict__ b,
+                            const uint8_t *__restrict__ y, int n, int Hh, float *__restrict__ prob,
+                            float *__restrict__ dlogit, float *__restrict__ loss_acc) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  float l = 0.f;
+  if (i < n) {
+    float z = b[0];
+    for (int h = 0; h < Hh; ++h) z = fmaf(Hl[(size_t)i * Hh + h], w[h], z);
+    const float p = 1.f / (1.f + __expf(-z));
+    prob[i] = p;
+    if (y) {
+      const float t = y[i] ? 1.f : 0.f;
+      // BCE with logits, stable form: max(z,0) - z t + log(1 + e^-|z|)
+      l = fmaxf(z, 0.f) - z * t + log1pf(__expf(-fabsf(z)));
+      dlogit[i] = (p - t) / (float)n;
+    }
+  }
+  if (y && loss_acc) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) l += __shfl_xor_sync(0xffffffffu, l, off);
+    if ((threadIdx.x & 31) == 0) atomicAdd(loss_acc, l / (float)n);
+  }
+}
+
+// dW[K x Hh] += A^T dZ (A: n x K, dZ: n x Hh); one thread per (k, h).
+__global__ void weight_grad_kernel(const float *__restrict__ A, const float *__restrict__ dZ, int n, int K, int Hh,
+                                   float *__restrict__ dW) {
+  const int k = blockIdx.x, h = threadIdx.x;
+  if (k >= K || h >= Hh) return;
+  float acc = 0.f;
+  for (int i = 0; i < n; ++i) acc = fmaf(A[(size_t)i * K + k], dZ[(size_t)i * Hh + h], acc);
+  dW[(size_t)k * Hh + h] += acc;
+}
+
+__global__ void bias_grad_kernel(const float *__restrict__ dZ, int n, int Hh, float *__restrict__ db) {
+  const int h = threadIdx.x;
+  if (h >= Hh) return;
+  float acc = 0.f;
+  for (int i = 0; i < n; ++i) acc += dZ[(size_t)i * Hh + h];
+  db[h] += acc;
+}
+
+// dZ = dH * (pre > 0)
+__global__ void relu_back_kernel(const float *__restrict__ dH, const float *__restrict__ pre, size_t count,
+                                 float *__restrict__ dZ) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < count) dZ[i] = pre[i] > 0.f ? dH[i] : 0.f;
+}
+
+// out[n x K] = dZ[n x Hh] W^T (W: K x Hh)  (+= when accumulate)
+__global__ void linear_back_kernel(const float *__restrict__ dZ, const float *__restrict__ W, int n, int K, int Hh,
+                                   int accumulate, float *__restrict__ out) {
+  const int i = blockIdx.x, k = threadIdx.x;
+  if (i >= n || k >= K) return;
+  float acc = 0.f;
+  for (int h = 0; h < Hh; ++h) acc = fmaf(dZ[(size_t)i * Hh + h], W[(size_t)k * Hh + h], acc);
+  out[(size_t)i * K + k] = accumulate ? out[(size_t)i * K + k] + acc : acc;
+}
+
+// dH_last = dlogit w_out^T ; dw_out += H^T dlogit ; db_out += sum dlogit
+__global__ void head_back_kernel(const float *__restrict__ Hl, const float *__restrict__ dlogit,
+                                 const float *__restrict__ w, int n, int Hh, float *__restrict__ dH,
+                                 float *__restrict__ dw, float *__restrict__ db) {
+  const int h = threadIdx.x;
+  if (blockIdx.x == 0 && h < Hh) {
+    float acc = 0.f;
+    for (int i = 0; i < n; ++i) acc = fmaf(Hl[(size_t)i * Hh + h], dlogit[i], acc);
+    dw[h] += acc;
+  }
+  if (blockIdx.x == 0 && h == 0) {
+    float s = 0.f;
+    for (int i = 0; i < n; ++i) s += dlogit[i];
+    db[0] += s;
+  }
+  for (int i = blockIdx.x; i < n; i += gridDim.x)
+    if (h < Hh) dH[(size_t)i * Hh + h] = dlogit[i] * w[h];
+}
+
+__global__ void add_kernel(float *__restrict__ a, const float *__restrict__ b, size_t count) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < count) a[i] += b[i];
+}
+
+__global__ void adam_kernel(float *__restrict__ p, const float *__restrict__ g, float *__restrict__ m,
+                            float *__restrict__ v, size_t count, float lr, float b1, float b2, float eps, float c1,
+                            float c2) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= count) return;
+  const float gi = g[i];
+  const float mi = b1 * m[i] + (1.f - b1) * gi;
+  const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+  m[i] = mi;
+  v[i] = vi;
+  p[i] -= lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+}
+
+}  // namespace mpnn
+}  // namespace os
+
+using namespace os;
+using namespace os::mpnn;
+
+// One stored instance: scaled couplings (BF16, padded to np x np), features,
+// optional labels.
+struct MpnnInstance {
+  int n = 0, np = 0;
+  DevBuf<__nv_bfloat16> c;
+  DevBuf<float> x;     // n x FEAT
+  DevBuf<uint8_t> y;   // n (oriented labels) or empty
+};
+
+struct os_mpnn {
+  os_ctx *ctx = nullptr;
+  int H = 64, L = 3;
+  bool orient = true;  // labels oriented with y_0 = 1
+  // parameter layout (FP32): W_in[FEAT*H], b_in[H], {Ws[H*H], Wm[H*H], b[H]} x L, w_out[H], b_out[1]
+  size_t nparam = 0;
+  DevBuf<float> param, grad, adam_m, adam_v;
+  long long adam_t = 0;
+  std::vector<std::unique_ptr<MpnnInstance>> inst;
+  // work buffers for n up to cap
+  int cap = 0;
+  DevBuf<float> X0pre, Hs, pres, M, dH, dZ, dM, prob, dlogit, loss;
+  DevBuf<__nv_bfloat16> Hb;
+
+  size_t off_win() const { return 0; }
+  size_t off_bin() const { return (size_t)FEAT * H; }
+  size_t off_layer(int l) const { return off_bin() + H + (size_t)l * (2 * H * H + H); }
+  size_t off_wout() const { return off_layer(L); }
+  size_t off_bout() const { return off_wout() + H; }
+};
+
+namespace {
+
+void ensure_work(os_mpnn *m, int np) {
+  if (np <= m->cap) return;
+  const size_t nh = (size_t)np * m->H;
+  m->X0pre.alloc(nh);
+  m->Hs.alloc(nh * (m->L + 1));
+  m->pres.alloc(nh * (m->L + 1));
+  m->M.alloc(nh * m->L);
+  m->dH.alloc(nh);
+  m->dZ.alloc(nh);
+  m->dM.alloc(nh);
+  m->prob.alloc(np);
+  m->dlogit.alloc(np);
+  m->loss.alloc(1);
+  m->Hb.alloc(nh);
+  m->cap = np;
+}
+
+// Forward pass of instance `in` (activations kept for the backward pass).
+void forward(os_mpnn *m, MpnnInstance &in, cudaStream_t s) {
+  const int n = in.n, np = in.np, H = m->H;
+  const size_t nh = (size_t)np * H;
+  float *P = m->param.get();
+  OS_CUDA(cudaMemsetAsync(m->Hs.get(), 0, sizeof(float) * nh * (m->L + 1), s));
+  // H0 = relu(X W_in + b_in)
+  linear_kernel<<<n, H, 0, s>>>(in.x.get(), P + m->off_win(), nullptr, nullptr, P + m->off_bin(), n, FEAT, H, 1,
+                                m->pres.get(), m->Hs.get());
+  for (int l = 0; l < m->L; ++l) {
+    const float *Hprev = m->Hs.get() + (size_t)l * nh;
+    float *Ml = m->M.get() + (size_t)l * nh;
+    to_bf16_kernel<<<(unsigned)ceil_div_u64(nh, 256), 256, 0, s>>>(Hprev, m->Hb.get(), nh);
+    gemm_ch_kernel<<<(np + GM - 1) / GM, 128, 0, s>>>(in.c.get(), np, m->Hb.get(), Ml);
+    const float *Wl = P + m->off_layer(l);
+    linear_kernel<<<n, H, 0, s>>>(Hprev, Wl, Ml, Wl + (size_t)H * H, Wl + 2 * (size_t)H * H, n, H, H, 1,
+                                  m->pres.get() + (size_t)(l + 1) * nh, m->Hs.get() + (size_t)(l + 1) * nh);
+  }
+  OS_CUDA(cudaGetLastError());
+}
+
+// Loss and gradients (accumulated into m->grad) of one instance; the
+// forward pass must have run. Element-wise work covers the n real rows; the
+// padded rows of the BF16 operands are zero.
+void backward(os_mpnn *m, MpnnInstance &in, cudaStream_t s) {
+  const int n = in.n, np = in.np, H = m->H;
+  const size_t nh = (size_t)np * H, rh = (size_t)n * H;
+  const unsigned eb = (unsigned)ceil_div_u64(rh, 256);
+  float *P = m->param.get(), *Gd = m->grad.get();
+  const float *HL = m->Hs.get() + (size_t)m->L * nh;
+  head_kernel<<<(n + 255) / 256, 256, 0, s>>>(HL, P + m->off_wout(), P + m->off_bout(), in.y.get(), n, H,
+                                              m->prob.get(), m->dlogit.get(), m->loss.get());
+  head_back_kernel<<<64, H, 0, s>>>(HL, m->dlogit.get(), P + m->off_wout(), n, H, m->dH.get(),
+                                    Gd + m->off_wout(), Gd + m->off_bout());
+  for (int l = m->L - 1; l >= 0; --l) {
+    const float *Hprev = m->Hs.get() + (size_t)l * nh;
+    const float *pre = m->pres.get() + (size_t)(l + 1) * nh;
+    const float *Ml = m->M.get() + (size_t)l * nh;
+    const float *Wl = P + m->off_layer(l);
+    float *Gl = Gd + m->off_layer(l);
+    relu_back_kernel<<<eb, 256, 0, s>>>(m->dH.get(), pre, rh, m->dZ.get());
+    weight_grad_kernel<<<H, H, 0, s>>>(Hprev, m->dZ.get(), n, H, H, Gl);               // dWs
+    weight_grad_kernel<<<H, H, 0, s>>>(Ml, m->dZ.get(), n, H, H, Gl + (size_t)H * H);  // dWm
+    bias_grad_kernel<<<1, H, 0, s>>>(m->dZ.get(), n, H, Gl + 2 * (size_t)H * H);        // db
+    // dM = dZ Wm^T ; dH_prev = dZ Ws^T + C^ dM  (C^ is symmetric)
+    linear_back_kernel<<<n, H, 0, s>>>(m->dZ.get(), Wl + (size_t)H * H, n, H, H, 0, m->dM.get());
+    linear_back_kernel<<<n, H, 0, s>>>(m->dZ.get(), Wl, n, H, H, 0, m->dH.get());
+    OS_CUDA(cudaMemsetAsync(m->Hb.get(), 0, sizeof(__nv_bfloat16) * nh, s));
+    to_bf16_kernel<<<eb, 256, 0, s>>>(m->dM.get(), m->Hb.get(), rh);
+    gemm_ch_kernel<<<(np + GM - 1) / GM, 128, 0, s>>>(in.c.get(), np, m->Hb.get(), m->dZ.get());
+    add_kernel<<<eb, 256, 0, s>>>(m->dH.get(), m->dZ.get(), rh);
+  }
+  // Input layer: dZ0 = dH0 * (pre0 > 0); dW_in = X^T dZ0; db_in = sum dZ0.
+  relu_back_kernel<<<eb, 256, 0, s>>>(m->dH.get(), m->pres.get(), rh, m->dZ.get());
+  weight_grad_kernel<<<FEAT, H, 0, s>>>(in.x.get(), m->dZ.get(), n, FEAT, H, Gd + m->off_win());
+  bias_grad_kernel<<<1, H, 0, s>>>(m->dZ.get(), n, H, Gd + m->off_bin());
+  OS_CUDA(cudaGetLastError());
+}
+
+// Stage an instance: scaled BF16 couplings, features, oriented labels.
+std::unique_ptr<MpnnInstance> stage(const os_qubo_dense *q, const char *label, bool orient) {
+  const int n = q->n;
+  OS_REQUIRE(n >= 2 && n <= 8192, "the network takes 2..8192 spins (got %d)", n);
+  auto in = std::make_unique<MpnnInstance>();
+  in->n = n;
+  in->np = (n + 63) / 64 * 64;
+  double ss = 0.0;
+  long long cnt = 0;
+  for (int i = 0; i < n; ++i)
+    for (int j = i + 1; j < n; ++j) {
+      const double v = q->f[(size_t)i * n + j];
+      OS_REQUIRE(std::isfinite(v), "coefficient (%d,%d) is not finite", i, j);
+      ss += v * v;
+      ++cnt;
+    }
+  const double rms = cnt ? std::sqrt(ss / cnt) : 0.0;
+  const double scale = rms > 0 ? rms * std::sqrt((double)n) : 1.0;
+  std::vector<__nv_bfloat16> c((size_t)in->np * in->np, __float2bfloat16(0.f));
+  std::vector<float> x((size_t)n * FEAT);
+  for (int i = 0; i < n; ++i) {
+    double rowsum = 0.0;
+    for (int j = 0; j < n; ++j) {
+      if (i == j) continue;
+      const double v = i < j ? q->f[(size_t)i * n + j] : q->f[(size_t)j * n + i];
+      rowsum += v;
+      c[(size_t)i * in->np + j] = __float2bfloat16((float)(v / scale));
+    }
+    x[(size_t)i * FEAT + 0] = 1.f;
+    x[(size_t)i * FEAT + 1] = (float)(q->f[(size_t)i * n + i] / scale);
+    x[(size_t)i * FEAT + 2] = (float)(rowsum / scale);
+    x[(size_t)i * FEAT + 3] = i == 0 ? 1.f : 0.f;
+  }
+  in->c.alloc(c.size());
+  OS_CUDA(cudaMemcpy(in->c.get(), c.data(), sizeof(__nv_bfloat16) * c.size(), cudaMemcpyHostToDevice));
+  in->x.alloc(x.size());
+  OS_CUDA(cudaMemcpy(in->x.get(), x.data(), sizeof(float) * x.size(), cudaMemcpyHostToDevice));
+  if (label) {
+    std::vector<uint8_t> y(n);
+    const bool flip = orient && label[0] == 0;  // orient so that y_0 = 1
+    for (int i = 0; i < n; ++i) y[i] = (uint8_t)((label[i] != 0) != flip);
+    in->y.alloc(n);
+    OS_CUDA(cudaMemcpy(in->y.get(), y.data(), n, cudaMemcpyHostToDevice));
+  }
+  return in;
+}
+
+void init_params(os_mpnn *m, unsigned long long seed) {
+  std::vector<float> p(m->nparam, 0.f);
+  // Scaled uniform initialisation from Philox (fan-in scaling).
+  size_t ctr = 0;
+  auto fill = [&](size_t off, int rows, int cols) {
+    const float a = std::sqrt(6.f / (float)(rows + cols));
+    for (int i = 0; i < rows * cols; ++i, ++ctr) {
+      Philox4 r = philox4x32_10((uint32_t)ctr, (uint32_t)(ctr >> 32), 0x11u, 0x4D504E4Eu, (uint32_t)seed,
+                                (uint32_t)(seed >> 32));
+      const float u = ((r.x >> 8) + 0.5f) * 0x1.0p-24f;
+      p[off + i] = a * (2.f * u - 1.f);
+    }
+  };
+  fill(m->off_win(), FEAT, m->H);
+  for (int l = 0; l < m->L; ++l) {
+    fill(m->off_layer(l), m->H, m->H);
+    fill(m->off_layer(l) + (size_t)m->H * m->H, m->H, m->H);
+  }
+  fill(m->off_wout(), m->H, 1);
+  OS_CUDA(cudaMemcpy(m->param.get(), p.data(), sizeof(float) * p.size(), cudaMemcpyHostToDevice));
+  OS_CUDA(cudaMemset(m->adam_m.get(), 0, sizeof(float) * m->nparam));
+  OS_CUDA(cudaMemset(m->adam_v.get(), 0, sizeof(float) * m->nparam));
+  m->adam_t = 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+os_status os_mpnn_create(os_ctx *ctx, int32_t hidden, int32_t layers, int32_t orient, uint64_t seed,
+                         os_mpnn **out) {
+  return guard([&] {
+    activate(ctx);
+    OS_REQUIRE(out != nullptr, "null output");
+    OS_REQUIRE(hidden == 64, "the message-passing kernels are built for 64 hidden units");
+    OS_REQUIRE(layers >= 1 && layers <= 8, "layers must be 1..8");
+    auto *m = new os_mpnn();
+    try {
+      m->ctx = ctx;
+      m->H = hidden;
+      m->L = layers;
+      m->orient = orient != 0;
+      m->nparam = m->off_bout() + 1;
+      m->param.alloc(m->nparam);
+      m->grad.alloc(m->nparam);
+      m->adam_m.alloc(m->nparam);
+      m->adam_v.alloc(m->nparam);
+      init_params(m, seed);
+    } catch (...) {
+      delete m;
+      throw;
+    }
+    *out = m;
+  });
+}
+
+void os_mpnn_destroy(os_mpnn *m) {
+  if (!m) return;
+  cudaSetDevice(m->ctx->device);
+  cudaStreamSynchronize(m->ctx->stream);
+  delete m;
+}
+
+int64_t os_mpnn_num_params(const os_mpnn *m) { return m ? (int64_t)m->nparam : -1; }
+
+os_status os_mpnn_get_params(os_mpnn *m, float *out, size_t cap) {
+  return guard([&] {
+    OS_REQUIRE(m && out && cap >= m->nparam, "buffer holds %zu values, %zu needed", cap, m ? m->nparam : 0);
+    activate(m->ctx);
+    OS_CUDA(cudaStreamSynchronize(m->ctx->stream));
+    OS_CUDA(cudaMemcpy(out, m->param.get(), sizeof(float) * m->nparam, cudaMemcpyDeviceToHost));
+  });
+}
+
+os_status os_mpnn_set_params(os_mpnn *m, const float *in, size_t count) {
+  return guard([&] {
+    OS_REQUIRE(m && in && count == m->nparam, "expected %zu parameters", m ? m->nparam : 0);
+    activate(m->ctx);
+    OS_CUDA(cudaStreamSynchronize(m->ctx->stream));
+    OS_CUDA(cudaMemcpy(m->param.get(), in, sizeof(float) * count, cudaMemcpyHostToDevice));
+  });
+}
+
+os_status os_mpnn_add_instance(os_mpnn *m, const os_qubo_dense *q, const char *label, int32_t *index) {
+  return guard([&] {
+    OS_REQUIRE(m && q && q->f, "null argument");
+    activate(m->ctx);
+    m->inst.push_back(stage(q, label, m->orient));
+    if (index) *index = (int32_t)m->inst.size() - 1;
+  });
+}
+
+os_status os_mpnn_clear_instances(os_mpnn *m) {
+  return guard([&] {
+    OS_REQUIRE(m != nullptr, "null model");
+    activate(m->ctx);
+    OS_CUDA(cudaStreamSynchronize(m->ctx->stream));
+    m->inst.clear();
+  });
+}
+
+os_status os_mpnn_loss_grad(os_mpnn *m, int32_t index, float *loss, float *grads, size_t cap) {
+  return guard([&] {
+    OS_REQUIRE(m && index >= 0 && index < (int)m->inst.size(), "no instance %d", index);
+    MpnnInstance &in = *m->inst[index];
+    OS_REQUIRE(in.y.count, "instance %d has no labels", index);
+    activate(m->ctx);
+    cudaStream_t s = m->ctx->stream;
+    ensure_work(m, in.np);
+    OS_CUDA(cudaMemsetAsync(m->grad.get(), 0, sizeof(float) * m->nparam, s));
+    OS_CUDA(cudaMemsetAsync(m->loss.get(), 0, sizeof(float), s));
+    forward(m, in, s);
+    backward(m, in, s);
+    if (loss) OS_CUDA(cudaMemcpyAsync(loss, m->loss.get(), sizeof(float), cudaMemcpyDeviceToHost, s));
+    if (grads) {
+      OS_REQUIRE(cap >= m->nparam, "gradient buffer too small");
+      OS_CUDA(cudaMemcpyAsync(grads, m->grad.get(), sizeof(float) * m->nparam, cudaMemcpyDeviceToHost, s));
+    }
+    OS_CUDA(cudaStreamSynchronize(s));
+  });
+}
+
+os_status os_mpnn_train(os_mpnn *m, int32_t epochs, float lr, uint64_t shuffle_seed, float *epoch_loss) {
+  return guard([&] {
+    OS_REQUIRE(m && epochs >= 0 && lr > 0.f, "bad arguments");
+    activate(m->ctx);
+    cudaStream_t s = m->ctx->stream;
+    std::vector<int> order;
+    for (int i = 0; i < (int)m->inst.size(); ++i)
+      if (m->inst[i]->y.count) order.push_back(i);
+    OS_REQUIRE(!order.empty(), "no labelled instances");
+    int npmax = 0;
+    for (int i : order) npmax = std::max(npmax, m->inst[i]->np);
+    ensure_work(m, npmax);
+    const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
+    unsigned long long st = shuffle_seed * 0x9E3779B97F4A7C15ull + 1;
+    for (int e = 0; e < epochs; ++e) {
+      for (size_t i = order.size(); i > 1; --i) {  // Fisher-Yates with a splitmix stream
+        st += 0x9E3779B97F4A7C15ull;
+        unsigned long long z = st;
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+        z ^= z >> 31;
+        std::swap(order[i - 1], order[z % i]);
+      }
+      OS_CUDA(cudaMemsetAsync(m->loss.get(), 0, sizeof(float), s));
+      for (int idx : order) {
+        MpnnInstance &in = *m->inst[idx];
+        OS_CUDA(cudaMemsetAsync(m->grad.get(), 0, sizeof(float) * m->nparam, s));
+        forward(m, in, s);
+        backward(m, in, s);
+        ++m->adam_t;
+        const float c1 = 1.f - std::pow(b1, (float)m->adam_t), c2 = 1.f - std::pow(b2, (float)m->adam_t);
+        adam_kernel<<<(unsigned)ceil_div_u64(m->nparam, 256), 256, 0, s>>>(
+            m->param.get(), m->grad.get(), m->adam_m.get(), m->adam_v.get(), m->nparam, lr, b1, b2, eps, c1, c2);
+        OS_CUDA(cudaGetLastError());
+      }
+      if (epoch_loss) {
+        float l = 0.f;
+        OS_CUDA(cudaMemcpyAsync(&l, m->loss.get(), sizeof(float), cudaMemcpyDeviceToHost, s));
+        OS_CUDA(cudaStreamSynchronize(s));
+        epoch_loss[e] = l / (float)order.size();
+      }
+    }
+    OS_CUDA(cudaStreamSynchronize(s));
+  });
+}
+
+os_status os_mpnn_predict(os_mpnn *m, const os_qubo_dense *q, float *prob) {
+  return guard([&] {
+    OS_REQUIRE(m && q && q->f && prob, "null argument");
+    activate(m->ctx);
+    cudaStream_t s = m->ctx->stream;
+    auto in = stage(q, nullptr, m->orient);
+    ensure_work(m, in->np);
+    forward(m, *in, s);
+    const float *HL = m->Hs.get() + (size_t)m->L * in->np * m->H;
+    float *P = m->param.get();
+    head_kernel<<<(in->n + 255) / 256, 256, 0, s>>>(HL, P + m->off_wout(), P + m->off_bout(), nullptr, in->n, m->H,
+                                                    m->prob.get(), nullptr, nullptr);
+    OS_CUDA(cudaGetLastError());
+    OS_CUDA(cudaMemcpyAsync(prob, m->prob.get(), sizeof(float) * in->n, cudaMemcpyDeviceToHost, s));
+    OS_CUDA(cudaStreamSynchronize(s));
+  });
+}
+
+}  // extern "C"

@@ -1,0 +1,112 @@
+"""Learned warm start for simulated annealing: data, training, gate, evaluation.
+
+Workflow (all annealing and all network arithmetic run on the GPU through
+the C ABI):
+
+1. ``sk_qubo(n, seed)`` -- Sherrington-Kirkpatrick instances, J_ij ~ N(0, 1/n),
+   h = 0, as QUBOs (x = (s + 1) / 2, offset dropped).
+2. ``label_states(instances)`` -- the best state plain SA finds on each
+   training instance (one batched anneal).
+3. ``WarmStartNet.train`` -- Adam on the oriented labels.
+4. ``probe_gate`` -- a short probe anneal from the predicted probabilities and
+   from fair coins; the warm start is used only when it ends lower.
+5. ``time_to_target`` -- the sweep budget (and wall time) each method needs to
+   come within a relative gap of a target energy.
+
+Plain random-init SA is both the fallback and the judge: targets come from
+long plain runs and every comparison uses the same number of trajectories.
+"""
+from __future__ import annotations
+
+import math
+import time
+from dataclasses import dataclass, field
+from typing import Optional, Sequence
+
+import numpy as np
+
+from . import (ACCEPT_PHYSICAL, BatchedAnnealPlan, Context, WarmStartNet, anneal, default_context,
+               geometric_schedule)
+
+
+def sk_qubo(n: int, seed: int) -> np.ndarray:
+    """SK instance as a QUBO: Q_ij = 4 J_ij (i != j), Q_ii = -2 sum_j J_ij."""
+    rng = np.random.default_rng(seed)
+    J = np.triu(rng.normal(0.0, 1.0 / math.sqrt(n), size=(n, n)), 1)
+    Js = J + J.T
+    f = 4.0 * Js
+    np.fill_diagonal(f, -2.0 * Js.sum(axis=1))
+    return f
+
+
+def label_states(instances: Sequence[np.ndarray], *, num_tries: int = 64, sweeps: int = 500,
+                 beta_min: float = 0.1, beta_max: float = 5.0, seed: int = 11,
+                 ctx: Optional[Context] = None, chunk: int = 64) -> list[np.ndarray]:
+    """Best state found by plain SA on each instance (batched, `chunk` at a time)."""
+    ctx = ctx or default_context()
+    beta = geometric_schedule(beta_min, beta_max, sweeps)
+    out = []
+    for i in range(0, len(instances), chunk):
+        part = list(instances[i:i + chunk])
+        plan = BatchedAnnealPlan(part, beta, num_tries=num_tries, resync_every=max(1, sweeps // 2), seed=seed + i,
+                                 ctx=ctx)
+        plan.execute()
+        out.extend(r.state.copy() for r in plan.result())
+        plan.close()
+    return out
+
+
+def train_net(instances, labels, *, epochs: int = 20, lr: float = 2e-3, seed: int = 1, orient: bool = True,
+              ctx: Optional[Context] = None) -> tuple[WarmStartNet, np.ndarray]:
+    net = WarmStartNet(seed=seed, orient=orient, ctx=ctx)
+    for f, y in zip(instances, labels):
+        net.add(f, y)
+    hist = net.train(epochs, lr=lr, seed=seed)
+    net.clear()
+    return net, hist
+
+
+@dataclass
+class GateResult:
+    use_warm: bool
+    warm_energy: float
+    cold_energy: float
+
+
+def probe_gate(f: np.ndarray, prob: np.ndarray, *, sweeps: int = 50, num_tries: int = 128, seed: int = 5,
+               warm_beta_min: float = 1.0, beta_min: float = 0.1, beta_max: float = 5.0,
+               ctx: Optional[Context] = None) -> GateResult:
+    """Short probe anneals; the warm start is kept only if it ends lower."""
+    warm = anneal(f, geometric_schedule(warm_beta_min, beta_max, sweeps), num_tries=num_tries, site_order=1,
+                  acceptance=ACCEPT_PHYSICAL, init_prob=prob, seed=seed, ctx=ctx)
+    cold = anneal(f, geometric_schedule(beta_min, beta_max, sweeps), num_tries=num_tries, site_order=1,
+                  acceptance=ACCEPT_PHYSICAL, seed=seed, ctx=ctx)
+    return GateResult(warm.traj_energies.mean() < cold.traj_energies.mean(), float(warm.traj_energies.mean()),
+                      float(cold.traj_energies.mean()))
+
+
+@dataclass
+class TTT:
+    sweeps: Optional[int]          # smallest budget that reached the target (None: never)
+    seconds: Optional[float]       # wall time of that run
+    energies: dict = field(default_factory=dict)
+
+
+def time_to_target(f: np.ndarray, target: float, *, rel_gap: float = 0.005, init_prob=None,
+                   budgets: Sequence[int] = (50, 100, 200, 400, 800, 1600), num_tries: int = 512,
+                   beta_min: float = 0.1, beta_max: float = 5.0, seed: int = 21,
+                   ctx: Optional[Context] = None) -> TTT:
+    """Smallest sweep budget whose best energy is within rel_gap of target."""
+    thr = target + rel_gap * abs(target)
+    res = TTT(None, None)
+    for s in budgets:
+        beta = geometric_schedule(beta_min, beta_max, s)
+        t0 = time.perf_counter()
+        r = anneal(f, beta, num_tries=num_tries, site_order=1, acceptance=ACCEPT_PHYSICAL, init_prob=init_prob,
+                   resync_every=max(1, s // 2), seed=seed, ctx=ctx)
+        dt = time.perf_counter() - t0
+        res.energies[s] = r.energy
+        if r.energy <= thr:
+            res.sweeps, res.seconds = s, dt
+            break
+    return res
