@@ -444,15 +444,18 @@ def bench_learned(args, ctx, pg, rank, world):
                             site_order=1, acceptance=osg.ACCEPT_PHYSICAL, resync_every=500, seed=99,
                             ctx=ctx).energy
         prob = net.predict(f)
-        gate = ws.probe_gate(f, prob, ctx=ctx)
-        cold = ws.time_to_target(f, target, ctx=ctx)
+        gate = ws.probe_gate(f, prob, beta_min=1.0, ctx=ctx)
+        plain = ws.time_to_target(f, target, ctx=ctx)                       # config schedule, fair coins
+        cold = ws.time_to_target(f, target, beta_min=1.0, ctx=ctx)          # warm runs' schedule, fair coins
         warm = ws.time_to_target(f, target, init_prob=prob, beta_min=1.0, ctx=ctx)
         chosen = warm if gate.use_warm else cold
-        rows.append({"seed": 10000 + k, "target": target, "use_warm": gate.use_warm,
+        rows.append({"seed": 10000 + k, "target": target, "use_warm": bool(gate.use_warm),
                      "probe_warm": gate.warm_energy, "probe_cold": gate.cold_energy,
-                     "plain_sweeps": cold.sweeps, "plain_s": cold.seconds,
+                     "plain_sweeps": plain.sweeps, "plain_s": plain.seconds,
+                     "cold_sweeps": cold.sweeps, "cold_s": cold.seconds,
                      "warm_sweeps": warm.sweeps, "warm_s": warm.seconds,
-                     "chosen_s": chosen.seconds})
+                     "chosen_s": chosen.seconds,
+                     "prob_abs_dev": float(np.mean(np.abs(prob - 0.5)))})
     def med(key):
         v = [r[key] for r in rows if r[key] is not None]
         return statistics.median(v) if v else None
@@ -465,10 +468,14 @@ def bench_learned(args, ctx, pg, rank, world):
         "config": {"workload": f"SK n=1024 J~N(0,1/n); {args.learned_train} training instances (labels: plain "
                                f"batched SA 64 traj x 500 sweeps); {args.learned_eval} held-out seeds; target = "
                                f"best of plain SA 512 traj x {args.learned_target_sweeps} sweeps; 512 trajectories "
-                               "per time-to-target run; warm runs start at beta 1.0, plain at 0.1 (geometric to 5.0)",
+                               "per time-to-target run; plain = config schedule beta 0.1->5.0 from fair coins; the warm "
+                               "start and its control (fair coins) both run beta 1.0->5.0; the probe gate compares "
+                               "those two",
                    "network": "3 message-passing layers, hidden 64, BF16 mma.sync + FP32"},
-        "result": {"plain_median_s": med("plain_s"), "warm_median_s": med("warm_s"),
-                   "plain_success": succ("plain_s"), "warm_success": succ("warm_s"),
+        "result": {"plain_median_s": med("plain_s"), "cold_schedule_random_median_s": med("cold_s"),
+                   "warm_median_s": med("warm_s"),
+                   "network_gain": (med("cold_s") / med("warm_s")) if med("cold_s") and med("warm_s") else None,
+                   "plain_success": succ("plain_s"), "cold_success": succ("cold_s"), "warm_success": succ("warm_s"),
                    "gate_uses_warm": sum(r["use_warm"] for r in rows), "instances": rows,
                    "train_loss_first_last": [float(hist[0]), float(hist[-1])] if len(hist) else None,
                    "label_s": t_label, "train_s": t_train},
@@ -582,6 +589,12 @@ CONFIG_NAMES = {
 }
 
 
+def _json_default(o):
+    if hasattr(o, "item"):
+        return o.item()
+    return str(o)
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("--gpus", type=int, default=1)
@@ -607,7 +620,7 @@ def main():
     if args.impl == "reference":
         out = reference_arm(args, world, rank)
         if out is not None:
-            print(json.dumps(out))
+            print(json.dumps(out, default=_json_default))
         return
 
     import torch
@@ -660,7 +673,7 @@ def main():
         for k in ("roofline", "cpu_baseline", "e2e", "gpu_launches", "clocks", "result", "secondary"):
             if k in out:
                 line[k] = out[k]
-        print(json.dumps(line))
+        print(json.dumps(line, default=_json_default))
     ctx.close()
     if pg is not None:
         pg.destroy_process_group()

@@ -74,13 +74,14 @@ class GateResult:
 
 
 def probe_gate(f: np.ndarray, prob: np.ndarray, *, sweeps: int = 50, num_tries: int = 128, seed: int = 5,
-               warm_beta_min: float = 1.0, beta_min: float = 0.1, beta_max: float = 5.0,
-               ctx: Optional[Context] = None) -> GateResult:
-    """Short probe anneals; the warm start is kept only if it ends lower."""
-    warm = anneal(f, geometric_schedule(warm_beta_min, beta_max, sweeps), num_tries=num_tries, site_order=1,
-                  acceptance=ACCEPT_PHYSICAL, init_prob=prob, seed=seed, ctx=ctx)
-    cold = anneal(f, geometric_schedule(beta_min, beta_max, sweeps), num_tries=num_tries, site_order=1,
-                  acceptance=ACCEPT_PHYSICAL, seed=seed, ctx=ctx)
+               beta_min: float = 1.0, beta_max: float = 5.0, ctx: Optional[Context] = None) -> GateResult:
+    """Short probe anneals with the same schedule, from the predicted
+    probabilities and from fair coins; the warm start is kept only if it ends
+    lower on average."""
+    beta = geometric_schedule(beta_min, beta_max, sweeps)
+    warm = anneal(f, beta, num_tries=num_tries, site_order=1, acceptance=ACCEPT_PHYSICAL, init_prob=prob,
+                  seed=seed, ctx=ctx)
+    cold = anneal(f, beta, num_tries=num_tries, site_order=1, acceptance=ACCEPT_PHYSICAL, seed=seed + 1, ctx=ctx)
     return GateResult(warm.traj_energies.mean() < cold.traj_energies.mean(), float(warm.traj_energies.mean()),
                       float(cold.traj_energies.mean()))
 
