@@ -54,8 +54,6 @@ template <int SLOTS> void launch_batch_resync(const BatchResyncArgs &b, cudaStre
 
 #define OS_BATCH_DISPATCH(cls, fn, ...)                                  \
   switch (cls) {                                                         \
-    case 1: fn<1>(__VA_ARGS__); break;                                   \
-    case 2: fn<2>(__VA_ARGS__); break;                                   \
     case 4: fn<4>(__VA_ARGS__); break;                                   \
     case 8: fn<8>(__VA_ARGS__); break;                                   \
     case 16: fn<16>(__VA_ARGS__); break;                                 \

@@ -15,24 +15,33 @@ namespace sa {
 
 constexpr int MAX_DENSE_N = 2048;  // 64 field slots per lane
 
-// Dense instance staged for the sweep kernels. Sites are padded to
-// nslots * 32; padding sites have zero couplings and never flip.
+// Dense instance staged for the sweep kernels. Sites are padded to a
+// multiple of 128 (nslots = ld / 32 slots, a multiple of 4); padding sites
+// have zero couplings and never flip. The FP32 coupling rows are stored in
+// slot order: row p = s*32 + l holds the couplings of site
+// ((s >> 2) << 7) + (l << 2) + (s & 3) (the site lane l owns in slot s),
+// columns in site order.
 struct DenseHost {
   int n = 0, nslots = 0, ld = 0;
-  std::vector<float> c32;    // ld*ld couplings, zero diagonal, symmetric
+  std::vector<float> c32;    // ld*ld couplings, zero diagonal, rows in slot order
   std::vector<float> d32;    // ld diagonal (linear) terms
   std::vector<double> c64;   // ld*ld FP64 couplings, zero diagonal
   std::vector<double> d64;   // ld
   std::vector<double> f;     // n*n flattened matrix as given (re-score)
 };
 
-inline int slots_for(int n) { return (n + 31) / 32; }
+inline int slots_for(int n) { return (n + 127) / 128 * 4; }
 
-// Power-of-two slot count of the kernel instance that serves nslots.
+// Power-of-two slot count (>= 4) of the kernel instance that serves nslots.
 inline int slot_class(int nslots) {
-  int s = 1;
+  int s = 4;
   while (s < nslots) s <<= 1;
   return s;
+}
+
+inline int slot_site_host(int p) {
+  const int s = p >> 5, l = p & 31;
+  return ((s >> 2) << 7) + (l << 2) + (s & 3);
 }
 
 inline void stage_dense(const os_qubo_dense *q, DenseHost &h) {
@@ -55,8 +64,12 @@ inline void stage_dense(const os_qubo_dense *q, DenseHost &h) {
       const double v = q->f[(size_t)i * n + j];
       OS_REQUIRE(std::isfinite(v), "coefficient (%d,%d) is not finite", i, j);
       h.c64[i * ld + j] = h.c64[j * ld + i] = v;
-      h.c32[i * ld + j] = h.c32[j * ld + i] = (float)v;
     }
+  }
+  for (size_t p = 0; p < ld; ++p) {
+    const int site = slot_site_host((int)p);
+    if (site >= n) continue;
+    for (int j = 0; j < n; ++j) h.c32[p * ld + j] = (float)h.c64[(size_t)site * ld + j];
   }
 }
 

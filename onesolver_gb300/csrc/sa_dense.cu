@@ -111,8 +111,6 @@ template <int SLOTS> void launch_resync(const ResyncArgs &a, int warps, cudaStre
 
 #define OS_SLOT_DISPATCH(cls, fn, ...)                                  \
   switch (cls) {                                                        \
-    case 1: fn<1>(__VA_ARGS__); break;                                  \
-    case 2: fn<2>(__VA_ARGS__); break;                                  \
     case 4: fn<4>(__VA_ARGS__); break;                                  \
     case 8: fn<8>(__VA_ARGS__); break;                                  \
     case 16: fn<16>(__VA_ARGS__); break;                                \

@@ -8,18 +8,28 @@
 //   dE_k = (1 - 2 x_k) (Q_kk + h_k)
 // and an accepted flip adds +/- row k of the coupling matrix to the fields.
 //
-// Layout: one warp per trajectory. Lane l owns sites s*32 + l for the slots
-// s < nslots; their fields sit in registers (h[s]) and their spins in one
-// lane-private bitmask (bit s). The slot loop is unrolled so every register
-// index is a compile-time constant.
+// Layout: one warp per trajectory. Sites are grouped by 128; in group g lane
+// l owns the four consecutive sites g*128 + 4l + j (j = 0..3), and "slot"
+// s = 4g + j is the set of 32 sites { g*128 + 4l + j : l = 0..31 }. A lane's
+// fields sit in registers as FP32 pairs (slots 2q, 2q+1 in one 64-bit
+// register) and its spins in one bitmask (bit s). A flip's row update then
+// reads the lane's four coupling values of a group with one 128-bit load and
+// adds them with two paired FP32 FMAs (fma.rn.f32x2). The slot loop is
+// unrolled so every register index is a compile-time constant.
 //
-// Sequential sweeps: the 32 sites of a slot are decided together. Each lane
-// evaluates its own site with the current fields; a warp ballot of the
-// accepting lanes gives the next site in sweep order that flips. The fields
-// are updated with that site's row, and only the lanes after it re-evaluate
-// (the earlier lanes' decisions are final because nothing before them
-// changed). A slot therefore costs (1 + accepted flips) ballot rounds, and a
-// rejected attempt costs no field work.
+// Coupling rows are stored in slot order (row p = s*32 + l holds the
+// couplings of site slot_site(s, l), columns in site order), so the rows of
+// the sites of one slot are contiguous in memory.
+//
+// Sequential sweeps visit the slots in order and, within a slot, the lanes in
+// order: a fixed permutation of the sites inside each group of 128. The 32
+// sites of a slot are decided together: each lane evaluates its own site with
+// the current fields; a warp ballot of the accepting lanes gives the next
+// site in sweep order that flips. The fields are updated with that site's
+// row, and only the lanes after it re-evaluate (the earlier lanes' decisions
+// are final because nothing before them changed). A slot therefore costs
+// (1 + accepted flips) ballot rounds, and a rejected attempt costs no field
+// work.
 //
 // Acceptance uses the threshold form of the Metropolis test: with
 // u ~ U(0,1) from Philox, the reference rule exp((E - E') / beta) > u is
@@ -39,9 +49,17 @@ namespace sa {
 
 constexpr unsigned FULL = 0xffffffffu;
 
+// Site owned by `lane` in slot `s`.
+__host__ __device__ __forceinline__ int slot_site(int s, int lane) {
+  return ((s >> 2) << 7) + (lane << 2) + (s & 3);
+}
+// Slot and lane of a site.
+__host__ __device__ __forceinline__ int site_slot(int k) { return ((k >> 7) << 2) + (k & 3); }
+__host__ __device__ __forceinline__ int site_lane(int k) { return (k & 127) >> 2; }
+
 struct DenseArgs {
-  const float *c;          // ld x ld couplings (zero diagonal)
-  const float *diag;       // ld
+  const float *c;          // ld x ld couplings (zero diagonal), rows in slot order
+  const float *diag;       // ld, site order
   int n, nslots, ld;
   int spb;                 // steps per beta
   const double *beta;      // schedule (device)
@@ -50,7 +68,7 @@ struct DenseArgs {
   int traj_count;          // trajectories in this launch
   int traj_offset;         // global index of the first trajectory (RNG)
   uint32_t seed_lo, seed_hi, instance;
-  float *h;                // [traj][nslots][32]
+  float *h;                // [traj][nslots/2][32] FP32 pairs (slots 2q, 2q+1)
   unsigned long long *x;   // [traj][32] lane masks
   unsigned long long *xbest;
   float *e;                // [traj] tracked energy
@@ -69,18 +87,80 @@ __device__ __forceinline__ float threshold(float u, float b, int acceptance) {
   return acceptance == OS_ACCEPT_REFERENCE ? -b * l : -l / b;
 }
 
-// Sequential-order sweeps over [step_begin, step_end) for one trajectory per
-// warp.
+__device__ __forceinline__ unsigned long long splat2(float x) {
+  const unsigned long long u = __float_as_uint(x);
+  return (u << 32) | u;
+}
+
+// acc = a * b + acc on both FP32 halves.
+__device__ __forceinline__ void ffma2(unsigned long long &acc, unsigned long long a, unsigned long long b) {
+  asm("fma.rn.f32x2 %0, %1, %2, %0;" : "+l"(acc) : "l"(a), "l"(b));
+}
+
+// One lane's FP32 fields, as pairs.
+template <int SLOTS> struct Fields {
+  static_assert(SLOTS % 4 == 0, "slots come in groups of four");
+  unsigned long long p[SLOTS / 2];
+
+  __device__ __forceinline__ float get(int s) const {
+    return (s & 1) ? __uint_as_float((unsigned)(p[s >> 1] >> 32)) : __uint_as_float((unsigned)p[s >> 1]);
+  }
+  __device__ __forceinline__ void zero() {
+#pragma unroll
+    for (int q = 0; q < SLOTS / 2; ++q) p[q] = 0ull;
+  }
+  // Field pairs of trajectory t: [t][nslots/2][32] 64-bit words.
+  __device__ __forceinline__ static unsigned long long *base(float *h, long long t, int nslots, int lane) {
+    return reinterpret_cast<unsigned long long *>(h) + (size_t)t * (nslots / 2) * 32 + lane;
+  }
+  __device__ __forceinline__ void load(const unsigned long long *src, int nslots) {
+#pragma unroll
+    for (int q = 0; q < SLOTS / 2; ++q) p[q] = 2 * q < nslots ? src[q * 32] : 0ull;
+  }
+  __device__ __forceinline__ void store(unsigned long long *dst, int nslots) const {
+#pragma unroll
+    for (int q = 0; q < SLOTS / 2; ++q)
+      if (2 * q < nslots) dst[q * 32] = p[q];
+  }
+  // fields += sgn * row; `row_lane` = the row's first element + 4 * lane
+  // (shared memory: 128-bit shared loads).
+  __device__ __forceinline__ void add_row(const float *row_lane, float sgn, int nslots) {
+    const unsigned long long s2 = splat2(sgn);
+#pragma unroll
+    for (int g = 0; g < SLOTS / 4; ++g) {
+      if (4 * g < nslots) {
+        const ulonglong2 v = *reinterpret_cast<const ulonglong2 *>(row_lane + g * 128);
+        ffma2(p[2 * g], v.x, s2);
+        ffma2(p[2 * g + 1], v.y, s2);
+      }
+    }
+  }
+  // Same from global memory through the read-only path.
+  __device__ __forceinline__ void add_row_global(const float *row_lane, float sgn, int nslots) {
+    const unsigned long long s2 = splat2(sgn);
+#pragma unroll
+    for (int g = 0; g < SLOTS / 4; ++g) {
+      if (4 * g < nslots) {
+        const ulonglong2 v = __ldg(reinterpret_cast<const ulonglong2 *>(row_lane + g * 128));
+        ffma2(p[2 * g], v.x, s2);
+        ffma2(p[2 * g + 1], v.y, s2);
+      }
+    }
+  }
+};
+
+// Sequential-order sweeps over [step_begin, step_end), one trajectory per
+// warp, rows read from global memory (used when two staged row tiles do not
+// fit in shared memory).
 template <int SLOTS>
 __global__ void __launch_bounds__(128) sa_dense_seq_kernel(const __grid_constant__ DenseArgs a) {
   const int lane = threadIdx.x & 31;
   const int t = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   if (t >= a.traj_count) return;
   const int nslots = a.nslots;
-  float h[SLOTS];
-  float *hp = a.h + (size_t)t * nslots * 32 + lane;
-#pragma unroll
-  for (int s = 0; s < SLOTS; ++s) h[s] = s < nslots ? hp[s * 32] : 0.f;
+  Fields<SLOTS> F;
+  unsigned long long *hq = Fields<SLOTS>::base(a.h, t, nslots, lane);
+  F.load(hq, nslots);
   unsigned long long xl = a.x[(size_t)t * 32 + lane];
   unsigned long long xb = a.xbest[(size_t)t * 32 + lane];
   float E = a.e[t], Eb = a.ebest[t];
@@ -95,27 +175,22 @@ __global__ void __launch_bounds__(128) sa_dense_seq_kernel(const __grid_constant
     for (int s = 0; s < SLOTS; ++s) {
       if (s >= nslots) break;
       if ((s & 3) == 0)
-        r = philox4x32_10((uint32_t)((s >> 2) * 32 + lane), (uint32_t)step, tg, c3, a.seed_lo,
-                          a.seed_hi);
+        r = philox4x32_10((uint32_t)((s >> 2) * 32 + lane), (uint32_t)step, tg, c3, a.seed_lo, a.seed_hi);
       const float theta = threshold(select4(r, s & 3), b, a.acceptance);
-      const int site = s * 32 + lane;
+      const int site = slot_site(s, lane);
       const bool valid = site < a.n;
       const float d = a.diag[site];
       int p = 0;
       for (;;) {
         const bool xs = (xl >> s) & 1ull;
-        const float loc = d + h[s];
+        const float loc = d + F.get(s);
         const float dE = xs ? -loc : loc;
         const unsigned mask = __ballot_sync(FULL, valid && lane >= p && dE < theta);
         if (!mask) break;
         const int i = __ffs(mask) - 1;
         const float dEi = __shfl_sync(FULL, dE, i);
         const bool xi = __shfl_sync(FULL, xs, i);
-        const float sgn = xi ? -1.f : 1.f;
-        const float *row = a.c + (size_t)(s * 32 + i) * a.ld + lane;
-#pragma unroll
-        for (int s2 = 0; s2 < SLOTS; ++s2)
-          if (s2 < nslots) h[s2] = fmaf(sgn, __ldg(row + s2 * 32), h[s2]);
+        F.add_row_global(a.c + (size_t)(s * 32 + i) * a.ld + 4 * lane, xi ? -1.f : 1.f, nslots);
         if (lane == i) xl ^= 1ull << s;
         E += dEi;
         ++acc;
@@ -127,9 +202,7 @@ __global__ void __launch_bounds__(128) sa_dense_seq_kernel(const __grid_constant
       }
     }
   }
-#pragma unroll
-  for (int s = 0; s < SLOTS; ++s)
-    if (s < nslots) hp[s * 32] = h[s];
+  F.store(hq, nslots);
   a.x[(size_t)t * 32 + lane] = xl;
   a.xbest[(size_t)t * 32 + lane] = xb;
   if (lane == 0) {
@@ -147,10 +220,9 @@ __global__ void __launch_bounds__(128) sa_dense_rand_kernel(const __grid_constan
   const int t = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   if (t >= a.traj_count) return;
   const int nslots = a.nslots;
-  float h[SLOTS];
-  float *hp = a.h + (size_t)t * nslots * 32 + lane;
-#pragma unroll
-  for (int s = 0; s < SLOTS; ++s) h[s] = s < nslots ? hp[s * 32] : 0.f;
+  Fields<SLOTS> F;
+  unsigned long long *hq = Fields<SLOTS>::base(a.h, t, nslots, lane);
+  F.load(hq, nslots);
   unsigned long long xl = a.x[(size_t)t * 32 + lane];
   unsigned long long xb = a.xbest[(size_t)t * 32 + lane];
   float E = a.e[t], Eb = a.ebest[t];
@@ -167,22 +239,18 @@ __global__ void __launch_bounds__(128) sa_dense_rand_kernel(const __grid_constan
     const uint32_t wu = second ? r.w : r.y;
     const int k = (int)__umulhi(wk, (uint32_t)a.n);
     const float theta = threshold(u01_open(wu), b, a.acceptance);
-    const int slot = k >> 5, owner = k & 31;
+    const int slot = site_slot(k), owner = site_lane(k);
     float hv = 0.f;
 #pragma unroll
     for (int s = 0; s < SLOTS; ++s)
-      if (s == slot) hv = h[s];
+      if (s == slot) hv = F.get(s);
     const bool xs = (xl >> slot) & 1ull;
-    const float loc = a.diag[k] + hv;
+    const float loc = a.diag[slot_site(slot, lane)] + hv;
     const float dEl = xs ? -loc : loc;
     const float dE = __shfl_sync(FULL, dEl, owner);
     const bool xk = __shfl_sync(FULL, xs, owner);
     if (dE < theta) {
-      const float sgn = xk ? -1.f : 1.f;
-      const float *row = a.c + (size_t)k * a.ld + lane;
-#pragma unroll
-      for (int s2 = 0; s2 < SLOTS; ++s2)
-        if (s2 < nslots) h[s2] = fmaf(sgn, __ldg(row + s2 * 32), h[s2]);
+      F.add_row_global(a.c + (size_t)(slot * 32 + owner) * a.ld + 4 * lane, xk ? -1.f : 1.f, nslots);
       if (lane == owner) xl ^= 1ull << slot;
       E += dE;
       ++acc;
@@ -192,9 +260,7 @@ __global__ void __launch_bounds__(128) sa_dense_rand_kernel(const __grid_constan
       }
     }
   }
-#pragma unroll
-  for (int s = 0; s < SLOTS; ++s)
-    if (s < nslots) hp[s * 32] = h[s];
+  F.store(hq, nslots);
   a.x[(size_t)t * 32 + lane] = xl;
   a.xbest[(size_t)t * 32 + lane] = xb;
   if (lane == 0) {
@@ -234,20 +300,18 @@ __device__ __forceinline__ bool tile_item(const DenseArgs &a, float *tiles, uint
   const int halves = 2 * nslots;
   const long long total = (long long)(a.step_end - a.step_begin) * halves;
 
-  float h[SLOTS];
+  Fields<SLOTS> F;
   unsigned long long xl = 0, xb = 0;
   float E = 0.f, Eb = 0.f;
-  float *hp = a.h + (size_t)t * nslots * 32 + lane;
+  unsigned long long *hq = Fields<SLOTS>::base(a.h, t, nslots, lane);
   if (active) {
-#pragma unroll
-    for (int s = 0; s < SLOTS; ++s) h[s] = s < nslots ? hp[s * 32] : 0.f;
+    F.load(hq, nslots);
     xl = a.x[(size_t)t * 32 + lane];
     xb = a.xbest[(size_t)t * 32 + lane];
     E = a.e[t];
     Eb = a.ebest[t];
   } else {
-#pragma unroll
-    for (int s = 0; s < SLOTS; ++s) h[s] = 0.f;
+    F.zero();
   }
   unsigned long long acc = 0;
   const uint32_t tg = (uint32_t)(a.traj_offset + t);
@@ -273,7 +337,7 @@ __device__ __forceinline__ bool tile_item(const DenseArgs &a, float *tiles, uint
       if ((s & 3) == 0)
         r = philox4x32_10((uint32_t)((s >> 2) * 32 + lane), (uint32_t)step, tg, c3, a.seed_lo, a.seed_hi);
       const float theta = threshold(select4(r, s & 3), b, a.acceptance);
-      const int site = s * 32 + lane;
+      const int site = slot_site(s, lane);
       const bool valid = site < a.n;
       const float d = a.diag[site];
 #pragma unroll
@@ -286,18 +350,14 @@ __device__ __forceinline__ bool tile_item(const DenseArgs &a, float *tiles, uint
           const int pend = p + TILE_ROWS;
           for (;;) {
             const bool xs = (xl >> s) & 1ull;
-            const float loc = d + h[s];
+            const float loc = d + F.get(s);
             const float dE = xs ? -loc : loc;
             const unsigned mask = __ballot_sync(FULL, valid && lane >= p && lane < pend && dE < theta);
             if (!mask) break;
             const int i = __ffs(mask) - 1;
             const float dEi = __shfl_sync(FULL, dE, i);
             const bool xi = __shfl_sync(FULL, xs, i);
-            const float sgn = xi ? -1.f : 1.f;
-            const float *row = tile + (size_t)(i - half * TILE_ROWS) * ld + lane;
-#pragma unroll
-            for (int s2 = 0; s2 < SLOTS; ++s2)
-              if (s2 < nslots) h[s2] = fmaf(sgn, row[s2 * 32], h[s2]);
+            F.add_row(tile + (size_t)(i - half * TILE_ROWS) * ld + 4 * lane, xi ? -1.f : 1.f, nslots);
             if (lane == i) xl ^= 1ull << s;
             E += dEi;
             ++acc;
@@ -323,9 +383,7 @@ __device__ __forceinline__ bool tile_item(const DenseArgs &a, float *tiles, uint
     }
   }
   if (active) {
-#pragma unroll
-    for (int s = 0; s < SLOTS; ++s)
-      if (s < nslots) hp[s * 32] = h[s];
+    F.store(hq, nslots);
     a.x[(size_t)t * 32 + lane] = xl;
     a.xbest[(size_t)t * 32 + lane] = xb;
     if (lane == 0) {
@@ -440,7 +498,7 @@ __global__ void __launch_bounds__(512) sa_batch_tile_kernel(const __grid_constan
 }
 
 struct ResyncArgs {
-  const double *c64;       // ld x ld FP64 couplings (zero diagonal)
+  const double *c64;       // ld x ld FP64 couplings (zero diagonal), site order
   const double *d64;       // ld
   int n, nslots, ld;
   int init;                // 1: draw the initial spins first
@@ -472,7 +530,7 @@ __device__ __forceinline__ void resync_traj(const ResyncArgs &a, int t) {
     for (int s = 0; s < nslots; ++s) {
       if ((s & 3) == 0)
         r = philox4x32_10((uint32_t)((s >> 2) * 32 + lane), 0u, tg, c3, a.seed_lo, a.seed_hi);
-      const int site = s * 32 + lane;
+      const int site = slot_site(s, lane);
       if (site >= a.n) continue;
       const uint32_t w = (s & 3) == 0 ? r.x : (s & 3) == 1 ? r.y : (s & 3) == 2 ? r.z : r.w;
       bool bit = a.init_prob ? (u01_open(w) < a.init_prob[site]) : (w >> 31) != 0;
@@ -489,23 +547,30 @@ __device__ __forceinline__ void resync_traj(const ResyncArgs &a, int t) {
     while (m) {
       const int i = __ffs(m) - 1;
       m &= m - 1;
-      const double *row = a.c64 + (size_t)(s * 32 + i) * a.ld + lane;
+      const double *row = a.c64 + (size_t)slot_site(s, i) * a.ld + 4 * lane;
 #pragma unroll
       for (int s2 = 0; s2 < SLOTS; ++s2)
-        if (s2 < nslots) h64[s2] += row[s2 * 32];
+        if (s2 < nslots) h64[s2] += row[(s2 >> 2) * 128 + (s2 & 3)];
     }
   }
   double epart = 0.0, drift = 0.0;
-  float *hp = a.h + (size_t)t * nslots * 32 + lane;
+  unsigned long long *hq = Fields<SLOTS>::base(a.h, t, nslots, lane);
 #pragma unroll
-  for (int s = 0; s < SLOTS; ++s) {
-    if (s >= nslots) break;
-    const int site = s * 32 + lane;
-    if (site < a.n) {
-      if (!a.init) drift = fmax(drift, fabs((double)hp[s * 32] - h64[s]));
-      if ((xl >> s) & 1ull) epart += a.d64[site] + 0.5 * h64[s];
+  for (int q = 0; q < SLOTS / 2; ++q) {
+    if (2 * q >= nslots) break;
+    const unsigned long long old = hq[q * 32];
+#pragma unroll
+    for (int e = 0; e < 2; ++e) {
+      const int s = 2 * q + e;
+      const int site = slot_site(s, lane);
+      if (site < a.n) {
+        const float h32 = e ? __uint_as_float((unsigned)(old >> 32)) : __uint_as_float((unsigned)old);
+        if (!a.init) drift = fmax(drift, fabs((double)h32 - h64[s]));
+        if ((xl >> s) & 1ull) epart += a.d64[site] + 0.5 * h64[s];
+      }
     }
-    hp[s * 32] = (float)h64[s];
+    hq[q * 32] = ((unsigned long long)__float_as_uint((float)h64[2 * q + 1]) << 32) |
+                 __float_as_uint((float)h64[2 * q]);
   }
 #pragma unroll
   for (int off = 16; off > 0; off >>= 1) {
@@ -571,30 +636,35 @@ __global__ void __launch_bounds__(128) sa_batch_resync_kernel(const __grid_const
   resync_traj<SLOTS>(a, t);
 }
 
+// Spin of site k from the lane masks of one trajectory.
+__device__ __forceinline__ uint8_t spin_of(const unsigned long long *xm, int k) {
+  return (uint8_t)((xm[site_lane(k)] >> site_slot(k)) & 1ull);
+}
+
 // Batched best states -> bytes and FP64 re-score in the reference's order
 // (one warp per trajectory; lane 0 adds the set pairs in row-major order).
-static __global__ void sa_batch_rescore_kernel(const BatchInstance *__restrict__ inst, const int *__restrict__ traj_inst,
-                                        const long long *__restrict__ state_off, long long total,
-                                        const unsigned long long *__restrict__ xbest, uint8_t *__restrict__ states,
-                                        double *__restrict__ e64) {
+static __global__ void sa_batch_rescore_kernel(const BatchInstance *__restrict__ inst,
+                                               const int *__restrict__ traj_inst,
+                                               const long long *__restrict__ state_off, long long total,
+                                               const unsigned long long *__restrict__ xbest,
+                                               uint8_t *__restrict__ states, double *__restrict__ e64) {
   const long long gt = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   const int lane = threadIdx.x & 31;
   if (gt >= total) return;
   const BatchInstance in = inst[traj_inst[gt]];
   uint8_t *out = states + state_off[gt];
-  for (int site = lane; site < in.n; site += 32)
-    out[site] = (uint8_t)((xbest[gt * 32 + (site & 31)] >> (site >> 5)) & 1ull);
+  for (int site = lane; site < in.n; site += 32) out[site] = spin_of(xbest + gt * 32, site);
   __syncwarp();
   if (lane == 0) e64[gt] = rescore_energy(in.f, in.n, out);
 }
 
 // Best states as one byte per variable, for the FP64 re-score.
-static __global__ void unpack_states_kernel(const unsigned long long *__restrict__ xbest, int n,
-                                     int traj_count, uint8_t *__restrict__ out) {
+static __global__ void unpack_states_kernel(const unsigned long long *__restrict__ xbest, int n, int traj_count,
+                                            uint8_t *__restrict__ out) {
   const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= (size_t)traj_count * n) return;
   const int t = (int)(idx / n), site = (int)(idx % n);
-  out[idx] = (uint8_t)((xbest[(size_t)t * 32 + (site & 31)] >> (site >> 5)) & 1ull);
+  out[idx] = spin_of(xbest + (size_t)t * 32, site);
 }
 
 }  // namespace sa
