@@ -58,7 +58,7 @@ struct os_sa_plan {
   os::DevBuf<unsigned long long> x, xbest;
 
   // sparse
-  int ncolors = 0, nnz = 0, traj_per_cta = 0;
+  int ncolors = 0, nnz = 0, traj_per_cta = 0, deg_max = 1;
   os::DevBuf<int> row_ptr, col, color_sites, color_ptr;
   os::DevBuf<float> val32, diag32;
   os::DevBuf<double> val64, diag64;

@@ -38,7 +38,7 @@ struct SparseArgs {
   const float *diag;
   const int *color_sites;
   const int *color_ptr;
-  int ncolors, n;
+  int ncolors, n, deg_max;
   const double *beta;
   int spb, step_begin, step_end, acceptance;
   int T, traj_per_cta;
@@ -51,17 +51,57 @@ struct SparseArgs {
   unsigned long long *accepted;
 };
 
-__global__ void __launch_bounds__(512) sa_sparse_kernel(const __grid_constant__ SparseArgs a) {
+// Position of the r-th (0-based) set bit of m, r < popc(m): binary search
+// over halves of the remaining window by population count.
+__device__ __forceinline__ int nth_set_bit(unsigned m, int r) {
+  int pos = 0;
+#pragma unroll
+  for (int w = 16; w > 0; w >>= 1) {
+    const int c = __popc(m & ((1u << w) - 1u));
+    if (r >= c) {
+      r -= c;
+      m >>= w;
+      pos += w;
+    }
+  }
+  return pos;
+}
+
+// Warp-cooperative neighbour update. The accepted sites of the warp (mask
+// `M`, lane i holding site k_i with sign sgn_i) are taken `per` at a time;
+// lane l serves edge `le` of the `lr`-th site of each group (lr = l / deg_max,
+// le = l % deg_max, fixed per lane), so the field atomics run with nearly
+// full warps instead of one lane per accepted site.
+__device__ __forceinline__ void spread_updates(unsigned M, int k, float sgn, int per, int lr, int le,
+                                               const int *__restrict__ row_ptr, const int *__restrict__ col,
+                                               const float *__restrict__ val, float *h) {
+  const int cnt = __popc(M);
+  for (int g = 0; g < cnt; g += per) {
+    const int r = g + lr;
+    const bool on = lr < per && r < cnt;
+    const int src = nth_set_bit(M, on ? r : 0);
+    const int ks = __shfl_sync(0xffffffffu, k, src);
+    const float ss = __shfl_sync(0xffffffffu, sgn, src);
+    if (on) {
+      const int r0 = row_ptr[ks];
+      if (le < row_ptr[ks + 1] - r0) atomicAdd(&h[col[r0 + le]], ss * val[r0 + le]);
+    }
+  }
+}
+
+__global__ void __launch_bounds__(256, 8) sa_sparse_kernel(const __grid_constant__ SparseArgs a) {
   extern __shared__ unsigned char smem[];
   const int R = a.traj_per_cta;
-  const int tpt = blockDim.x / R;            // threads per trajectory
+  const int tpt = blockDim.x / R;            // threads per trajectory (multiple of 32)
   const int slot = threadIdx.x / tpt;        // trajectory within the CTA
   const int tid = threadIdx.x % tpt;
+  const int lane = threadIdx.x & 31;
   const int n = a.n;
   float *h_all = reinterpret_cast<float *>(smem);
   uint8_t *x_all = reinterpret_cast<uint8_t *>(h_all + (size_t)R * n);
-  __shared__ float s_de[16];
-  __shared__ int s_improve[16];
+  __shared__ float s_de[8];
+  __shared__ double s_e[8], s_eb[8];
+  __shared__ int s_improve[8];
   const int t = blockIdx.x * R + slot;
   const bool active = t < a.T;
   float *h = h_all + (size_t)slot * n;
@@ -72,71 +112,105 @@ __global__ void __launch_bounds__(512) sa_sparse_kernel(const __grid_constant__ 
       x[i] = a.x[(size_t)t * n + i];
     }
   }
-  if (threadIdx.x < 16) s_de[threadIdx.x] = 0.f;
+  if (tid == 0) {
+    s_de[slot] = 0.f;
+    s_e[slot] = active ? a.e[t] : 0.0;
+    s_eb[slot] = active ? a.ebest[t] : 0.0;
+  }
   __syncthreads();
-  double E = active ? a.e[t] : 0.0, Eb = active ? a.ebest[t] : 0.0;
-  unsigned long long acc = 0;
+  unsigned acc = 0;
   const uint32_t c3 = (a.instance & 0x0FFFFFFFu) | kStreamSweep;
+  const bool coop = a.deg_max <= 32;
+  const int per = coop ? 32 / a.deg_max : 0;
+  const int lr = coop ? lane / a.deg_max : 0, le = coop ? lane - lr * a.deg_max : 0;
   for (int step = a.step_begin; step < a.step_end; ++step) {
     const float b = (float)a.beta[step / a.spb];
     float de = 0.f;
     for (int c = 0; c < a.ncolors; ++c) {
       const int c0 = a.color_ptr[c], cnt = a.color_ptr[c + 1] - c0;
-      if (active) {
-        for (int base = tid; base < cnt; base += 4 * tpt) {
-          const Philox4 r = philox4x32_10((uint32_t)(c0 + base), (uint32_t)step, (uint32_t)t, c3,
-                                          a.seed_lo, a.seed_hi);
+      // Warp-uniform trip count (the warp's first thread decides), so that
+      // every lane takes part in the ballots; thread tid attempts the same
+      // sites with the same Philox counters as a per-thread loop would.
+      for (int wbase = tid - lane; wbase < cnt; wbase += 4 * tpt) {
+        const int mybase = wbase + lane;
+        const Philox4 r = philox4x32_10((uint32_t)(c0 + mybase), (uint32_t)step, (uint32_t)t, c3, a.seed_lo,
+                                        a.seed_hi);
 #pragma unroll
-          for (int m = 0; m < 4; ++m) {
-            const int idx = base + m * tpt;
-            if (idx >= cnt) break;
-            const int k = a.color_sites[c0 + idx];
+        for (int m = 0; m < 4; ++m) {
+          const int idx = mybase + m * tpt;
+          const bool valid = active && idx < cnt;
+          int k = 0;
+          bool accept = false;
+          float sgn = 0.f;
+          if (valid) {
+            k = a.color_sites[c0 + idx];
             const uint32_t w = m == 0 ? r.x : m == 1 ? r.y : m == 2 ? r.z : r.w;
             const float l = __logf(u01_open(w));
             const float theta = a.acceptance == OS_ACCEPT_REFERENCE ? -b * l : -l / b;
             const float loc = a.diag[k] + h[k];
             const bool xk = x[k];
             const float dE = xk ? -loc : loc;
-            if (dE < theta) {
+            accept = dE < theta;
+            if (accept) {
               x[k] = xk ? 0 : 1;
-              const float sgn = xk ? -1.f : 1.f;
-              const int e1 = a.row_ptr[k + 1];
-              for (int e = a.row_ptr[k]; e < e1; ++e) atomicAdd(&h[a.col[e]], sgn * a.val[e]);
+              sgn = xk ? -1.f : 1.f;
               de += dE;
               ++acc;
             }
           }
+          if (coop) {
+            const unsigned M = __ballot_sync(0xffffffffu, accept);
+            if (M) spread_updates(M, k, sgn, per, lr, le, a.row_ptr, a.col, a.val, h);
+          } else if (accept) {
+            const int e1 = a.row_ptr[k + 1];
+            for (int e = a.row_ptr[k]; e < e1; ++e) atomicAdd(&h[a.col[e]], sgn * a.val[e]);
+          }
         }
       }
-      __syncthreads();
+      if (c + 1 < a.ncolors) __syncthreads();
     }
-    // Sweep end: energy of each trajectory and best-state check.
+    // Sweep end: energy of each trajectory and best-state check. Each thread
+    // copies only the sites it attempts itself (colour index = tid mod tpt),
+    // which no other thread writes, so the copy needs no barrier after it.
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) de += __shfl_xor_sync(0xffffffffu, de, off);
-    if ((threadIdx.x & 31) == 0) atomicAdd(&s_de[slot], de);
+    if (lane == 0) atomicAdd(&s_de[slot], de);
     __syncthreads();
-    E += (double)s_de[slot];
-    const bool improve = active && E < Eb;
-    if (tid == 0) s_improve[slot] = improve;
-    __syncthreads();
-    if (threadIdx.x < 16) s_de[threadIdx.x] = 0.f;
-    if (s_improve[slot]) {
-      Eb = E;
-      for (int i = tid; i < n; i += tpt) a.xbest[(size_t)t * n + i] = x[i];
+    if (tid == 0) {
+      const double En = s_e[slot] + (double)s_de[slot];
+      const bool imp = active && En < s_eb[slot];
+      s_e[slot] = En;
+      if (imp) s_eb[slot] = En;
+      s_improve[slot] = imp;
+      s_de[slot] = 0.f;
     }
     __syncthreads();
+    if (s_improve[slot]) {
+      for (int c = 0; c < a.ncolors; ++c) {
+        const int c0 = a.color_ptr[c], cnt = a.color_ptr[c + 1] - c0;
+        for (int idx = tid; idx < cnt; idx += tpt) {
+          const int k = a.color_sites[c0 + idx];
+          a.xbest[(size_t)t * n + k] = x[k];
+        }
+      }
+    }
+    if (acc >= (1u << 30)) {
+      atomicAdd(&a.accepted[t], (unsigned long long)acc);
+      acc = 0;
+    }
   }
+  __syncthreads();
   if (active) {
     for (int i = tid; i < n; i += tpt) {
       a.h[(size_t)t * n + i] = h[i];
       a.x[(size_t)t * n + i] = x[i];
     }
     if (tid == 0) {
-      a.e[t] = E;
-      a.ebest[t] = Eb;
+      a.e[t] = s_e[slot];
+      a.ebest[t] = s_eb[slot];
     }
     // Accepted-flip count: one atomic per thread with flips.
-    if (acc) atomicAdd(&a.accepted[t], acc);
+    if (acc) atomicAdd(&a.accepted[t], (unsigned long long)acc);
   }
 }
 
@@ -326,6 +400,9 @@ void plan_create_sparse(os_sa_plan *p, const os_qubo_csr *q) {
   p->n = n;
   p->nnz = nnz;
   p->ncolors = nc;
+  p->deg_max = 0;
+  for (int i = 0; i < n; ++i) p->deg_max = std::max(p->deg_max, rp[i + 1] - rp[i]);
+  p->deg_max = std::max(p->deg_max, 1);
   p->row_ptr.alloc(n + 1);
   p->col.alloc(nnz);
   p->val32.alloc(nnz);
@@ -353,16 +430,16 @@ void plan_create_sparse(os_sa_plan *p, const os_qubo_csr *q) {
   p->accepted.alloc(T);
   p->states.alloc(T * n);
   p->e64.alloc(T);
-  // Threads per trajectory: enough to cover the largest colour in a few
-  // rounds; trajectories per CTA fill 512 threads within the shared memory.
+  // Threads per trajectory: one Philox call (four sites) per thread and
+  // colour where the largest colour allows, 32..256; a CTA has 256 threads
+  // (256 / tpt trajectories), eight CTAs per SM.
   int maxc = 1;
   for (int c = 0; c < nc; ++c) maxc = std::max(maxc, cptr[c + 1] - cptr[c]);
   int tpt = 32;
-  while (tpt < 256 && tpt * 8 < maxc) tpt <<= 1;
-  int R = 512 / tpt;
+  while (tpt < 256 && tpt * 4 < maxc) tpt <<= 1;
+  int R = 256 / tpt;
   const size_t per = (size_t)n * 5;
-  while (R > 1 && per * R > 160 * 1024) R >>= 1;
-  R = std::min(R, 16);
+  while (R > 1 && per * R > 100 * 1024) R >>= 1;  // R <= 8 (tpt >= 32)
   OS_REQUIRE(per <= 200 * 1024, "sparse instance too large for shared memory (%d variables)", n);
   p->traj_per_cta = R;
   p->warps = tpt * R / 32;
@@ -411,6 +488,7 @@ void execute_sparse(os_sa_plan *p) {
   a.color_ptr = p->color_ptr.get();
   a.ncolors = p->ncolors;
   a.n = n;
+  a.deg_max = p->deg_max;
   a.beta = p->beta.get();
   a.spb = p->spb;
   a.acceptance = p->acceptance;
