@@ -390,13 +390,15 @@ os_status os_mpnn_train(os_mpnn *model, int32_t epochs, float lr, uint64_t shuff
 /* Per-spin P(x_i = 1) (n floats) for a new instance. */
 os_status os_mpnn_predict(os_mpnn *model, const os_qubo_dense *qubo, float *prob);
 
-/* Measured roofline denominators for the two integer/FP32-bound paths (the
- * measured peaks cover HBM copy bandwidth and bf16 GEMMs only): the
- * INT32 issue rate of the enumeration's per-state instruction pair (three-
- * input add, integer min), in Gop/s, and the FP32 FMA rate, in GFLOP/s.
- * No reference counterpart. */
+/* Measured roofline denominators for the integer/FP32/shared-memory-bound
+ * paths (the measured peaks cover HBM copy bandwidth and bf16 GEMMs
+ * only): the INT32 issue rate of the enumeration's per-state instruction pair
+ * (three-input add, integer min), in Gop/s; the FP32 FMA rate, in GFLOP/s;
+ * and the shared-memory read rate of the annealing field update (128-bit
+ * shared loads feeding paired FP32 FMAs), in GB/s. No reference counterpart. */
 os_status os_probe_int32_peak(os_ctx *ctx, double *gops);
 os_status os_probe_fp32_fma_peak(os_ctx *ctx, double *gflops);
+os_status os_probe_smem_row_peak(os_ctx *ctx, double *gbs);
 
 #ifdef __cplusplus
 }

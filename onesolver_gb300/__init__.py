@@ -156,6 +156,7 @@ SIGNATURES = {
     "os_mpnn_predict": (C.c_int, [_P, C.POINTER(_QuboDense), C.POINTER(C.c_float)]),
     "os_probe_int32_peak": (C.c_int, [_P, C.POINTER(C.c_double)]),
     "os_probe_fp32_fma_peak": (C.c_int, [_P, C.POINTER(C.c_double)]),
+    "os_probe_smem_row_peak": (C.c_int, [_P, C.POINTER(C.c_double)]),
 }
 
 
@@ -594,6 +595,11 @@ class AnnealPlan:
     def launches(self) -> int:
         return int(lib().os_sa_plan_launches(self._h))
 
+    @property
+    def warps(self) -> int:
+        """Trajectories per CTA of the sweep launches (autotuned for staged tiles)."""
+        return int(lib().os_sa_plan_tuned_warps(self._h))
+
     def kernel_ms(self) -> float:
         """Device time of the last execute's sweep kernels (CUDA events)."""
         v = C.c_float()
@@ -823,6 +829,15 @@ def probe_fp32_fma_peak(ctx: Optional[Context] = None) -> float:
     ctx = ctx or default_context()
     v = C.c_double()
     _check(lib().os_probe_fp32_fma_peak(ctx.handle, C.byref(v)))
+    return v.value
+
+
+def probe_smem_row_peak(ctx: Optional[Context] = None) -> float:
+    """Measured shared-memory read rate of the dense field update (128-bit
+    shared loads feeding paired FP32 FMAs), GB/s."""
+    ctx = ctx or default_context()
+    v = C.c_double()
+    _check(lib().os_probe_smem_row_peak(ctx.handle, C.byref(v)))
     return v.value
 
 

@@ -8,9 +8,11 @@
 #include <cstdarg>
 #include <cstdint>
 #include <cstdio>
+#include <map>
 #include <new>
 #include <stdexcept>
 #include <string>
+#include <tuple>
 
 #include "onesolver.h"
 #include "errors.hpp"
@@ -61,6 +63,10 @@ struct os_ctx {
   int sm_count = 0;
   cudaStream_t own_stream = nullptr;
   cudaStream_t stream = nullptr;
+  // Tuned trajectories per CTA of the dense staged-tile sweep, keyed by
+  // (padded row length, trajectories, acceptance rule): later plans of the
+  // same shape reuse the choice instead of probing again.
+  std::map<std::tuple<int, int, int>, int> dense_warps;
 };
 
 namespace os {

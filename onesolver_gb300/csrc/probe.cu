@@ -1,7 +1,9 @@
 // probe.cu -- measured roofline denominators that the driver does not
 // provide: the INT32 issue rate of the exhaustive kernel's per-state
 // instruction pair (three-input add with a constant-bank operand, then an
-// integer min), and the FP32 FMA rate of the annealing field updates.
+// integer min), the FP32 FMA rate, and the shared-memory read rate of the
+// dense annealing row update (one 128-bit shared load feeding two paired FP32
+// FMAs per lane, the instruction pair of a field update).
 #include <cstdint>
 #include <utility>
 
@@ -72,6 +74,34 @@ __global__ void __launch_bounds__(256) fp32_probe_kernel(int iters, float a, flo
   if (r == 1234.5f) sink[0] = r;
 }
 
+// Per iteration: four 128-bit shared loads (64 bytes) and eight paired
+// FMAs per thread, from 16 rows of 512 floats (conflict-free: lane l reads
+// floats 4l..4l+3 of each 128-float group, like the dense field update).
+constexpr int ROW_PROBE_FLOATS = 16 * 512;
+__global__ void __launch_bounds__(256) smem_row_probe_kernel(int iters, float sgn, float *sink) {
+  __shared__ __align__(16) float buf[ROW_PROBE_FLOATS];
+  for (int i = threadIdx.x; i < ROW_PROBE_FLOATS; i += blockDim.x) buf[i] = (float)(i & 1023) * 1e-4f;
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const unsigned long long s2 = ((unsigned long long)__float_as_uint(sgn) << 32) | __float_as_uint(sgn);
+  unsigned long long acc[8];
+#pragma unroll
+  for (int j = 0; j < 8; ++j) acc[j] = 0ull;
+  for (int it = 0; it < iters; ++it) {
+    const float *row = buf + ((it * 7 + warp) & 15) * 512 + 4 * lane;
+#pragma unroll
+    for (int g = 0; g < 4; ++g) {
+      const ulonglong2 v = *reinterpret_cast<const ulonglong2 *>(row + g * 128);
+      asm("fma.rn.f32x2 %0, %1, %2, %0;" : "+l"(acc[2 * g]) : "l"(v.x), "l"(s2));
+      asm("fma.rn.f32x2 %0, %1, %2, %0;" : "+l"(acc[2 * g + 1]) : "l"(v.y), "l"(s2));
+    }
+  }
+  unsigned long long r = 0;
+#pragma unroll
+  for (int j = 0; j < 8; ++j) r ^= acc[j];
+  if (r == 0x123456789abcdefull) sink[0] = 1.f;
+}
+
 template <class F> double time_ms(cudaStream_t s, F &&launch) {
   cudaEvent_t e0, e1;
   OS_CUDA(cudaEventCreate(&e0));
@@ -134,6 +164,25 @@ os_status os_probe_fp32_fma_peak(os_ctx *ctx, double *gflops) {
     });
     const double flops = 2.0 * 64 * 8 * (double)iters * grid * 256.0;
     *gflops = flops / (ms * 1e-3) / 1e9;
+  });
+}
+
+os_status os_probe_smem_row_peak(os_ctx *ctx, double *gbs) {
+  return guard([&] {
+    activate(ctx);
+    OS_REQUIRE(gbs != nullptr, "null output");
+    DevBuf<float> sink;
+    sink.alloc(1);
+    int occ = 0;
+    OS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, smem_row_probe_kernel, 256, 0));
+    const int grid = ctx->sm_count * (occ > 0 ? occ : 1);
+    const int iters = 4096;
+    const double ms = time_ms(ctx->stream, [&] {
+      smem_row_probe_kernel<<<grid, 256, 0, ctx->stream>>>(iters, -1.f, sink.get());
+      OS_CUDA(cudaGetLastError());
+    });
+    const double bytes = 64.0 * (double)iters * grid * 256.0;
+    *gbs = bytes / (ms * 1e-3) / 1e9;
   });
 }
 

@@ -94,6 +94,7 @@ template <int SLOTS> void launch_seq(const DenseArgs &a, int warps, cudaStream_t
   sa_dense_seq_kernel<SLOTS><<<grid, warps * 32, 0, s>>>(a);
 }
 template <int SLOTS> void launch_tile(const DenseArgs &a, int warps, cudaStream_t s) {
+  // ceil(T / W) CTAs; each takes T / grid trajectories, rounded (<= W).
   const int grid = (a.traj_count + warps - 1) / warps;
   const size_t smem = (size_t)2 * TILE_ROWS * a.ld * sizeof(float);
   OS_CUDA(cudaFuncSetAttribute(sa_dense_tile_kernel<SLOTS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -185,18 +186,14 @@ void plan_create_dense(os_sa_plan *p, const os_qubo_dense *q) {
   p->status.alloc(1);
 }
 
-void execute_dense(os_sa_plan *p) {
-  cudaStream_t s = p->ctx->stream;
-  p->launches = 0;
-  OS_CUDA(cudaMemsetAsync(p->accepted.get(), 0, sizeof(unsigned long long) * p->T, s));
-  OS_CUDA(cudaMemsetAsync(p->drift.get(), 0, sizeof(unsigned long long), s));
+ResyncArgs dense_resync_args(os_sa_plan *p, int init) {
   ResyncArgs r{};
   r.c64 = p->c64.get();
   r.d64 = p->d64.get();
   r.n = p->n;
   r.nslots = p->nslots;
   r.ld = p->ld;
-  r.init = 1;
+  r.init = init;
   r.init_prob = p->init_prob.count ? p->init_prob.get() : nullptr;
   r.traj_count = p->T;
   r.traj_offset = 0;
@@ -209,9 +206,10 @@ void execute_dense(os_sa_plan *p) {
   r.e = p->e.get();
   r.ebest = p->ebest.get();
   r.drift_bits = p->drift.get();
-  dense_resync(r, p->slot_cls, p->warps, s);
-  ++p->launches;
+  return r;
+}
 
+DenseArgs dense_args(os_sa_plan *p) {
   DenseArgs a{};
   a.c = p->c32.get();
   a.diag = p->d32.get();
@@ -223,8 +221,8 @@ void execute_dense(os_sa_plan *p) {
   a.acceptance = p->acceptance;
   a.traj_count = p->T;
   a.traj_offset = 0;
-  a.seed_lo = r.seed_lo;
-  a.seed_hi = r.seed_hi;
+  a.seed_lo = (uint32_t)p->seed;
+  a.seed_hi = (uint32_t)(p->seed >> 32);
   a.instance = 0;
   a.h = p->h.get();
   a.x = p->x.get();
@@ -233,6 +231,61 @@ void execute_dense(os_sa_plan *p) {
   a.ebest = p->ebest.get();
   a.accepted = p->accepted.get();
   a.status = p->status.get();
+  return a;
+}
+
+// Trajectories per CTA of the staged-tile sweep: every CTA streams the whole
+// coupling matrix from L2 once per sweep, so more trajectories per CTA mean
+// less tile traffic but fewer SMs and more warps per scheduler. Time a few
+// sweeps of each candidate on the plan's own instance and keep the fastest
+// (execute re-initialises every trajectory afterwards).
+constexpr int DENSE_PROBE_STEPS = 8;
+int autotune_dense_warps(os_sa_plan *p) {
+  const int w0 = dense_warps(p->T, p->ctx->sm_count, true);
+  if (!p->tiled || p->T <= w0) return w0;
+  const auto key = std::make_tuple(p->ld, p->T, p->acceptance);
+  auto hit = p->ctx->dense_warps.find(key);
+  if (hit != p->ctx->dense_warps.end()) return hit->second;
+  cudaStream_t s = p->ctx->stream;
+  OS_CUDA(cudaMemsetAsync(p->status.get(), 0, sizeof(int), s));
+  dense_resync(dense_resync_args(p, 1), p->slot_cls, 4, s);
+  DenseArgs a = dense_args(p);
+  a.step_begin = 0;
+  a.step_end = std::min(DENSE_PROBE_STEPS, p->steps);
+  cudaEvent_t e0, e1;
+  OS_CUDA(cudaEventCreate(&e0));
+  OS_CUDA(cudaEventCreate(&e1));
+  int best_w = w0;
+  float best_ms = -1.f;
+  for (int W = w0; W <= 16 && W <= 4 * w0; W *= 2) {
+    OS_CUDA(cudaEventRecord(e0, s));
+    dense_sweeps(a, p->slot_cls, W, true, s);
+    OS_CUDA(cudaEventRecord(e1, s));
+    OS_CUDA(cudaEventSynchronize(e1));
+    float ms = 0.f;
+    OS_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+    if (best_ms < 0.f || ms < best_ms) {
+      best_w = W;
+      best_ms = ms;
+    }
+    if (W * 2 > p->T) break;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  p->ctx->dense_warps[key] = best_w;
+  return best_w;
+}
+
+void execute_dense(os_sa_plan *p) {
+  cudaStream_t s = p->ctx->stream;
+  p->launches = 0;
+  OS_CUDA(cudaMemsetAsync(p->accepted.get(), 0, sizeof(unsigned long long) * p->T, s));
+  OS_CUDA(cudaMemsetAsync(p->drift.get(), 0, sizeof(unsigned long long), s));
+  ResyncArgs r = dense_resync_args(p, 1);
+  dense_resync(r, p->slot_cls, p->warps, s);
+  ++p->launches;
+
+  DenseArgs a = dense_args(p);
   OS_CUDA(cudaMemsetAsync(p->status.get(), 0, sizeof(int), s));
   r.init = 0;
   const int chunk = p->chunk;
@@ -251,7 +304,7 @@ void execute_dense(os_sa_plan *p) {
   unpack_states_kernel<<<(unsigned)ceil_div_u64(total, 256), 256, 0, s>>>(p->xbest.get(), p->n, p->T,
                                                                         p->states.get());
   OS_CUDA(cudaGetLastError());
-  launch_rescore(p->f.get(), p->n, p->states.get(), p->T, p->e64.get(), s);
+  launch_rescore_warp(p->f.get(), p->n, p->states.get(), p->T, p->e64.get(), s);
   p->launches += 2;
 }
 
@@ -336,6 +389,7 @@ os_status os_sa_plan_create_dense(os_ctx *ctx, const os_qubo_dense *qubo, const 
       p->kind = 0;
       os_sa_plan_common(p, ctx, params, qubo->n);
       plan_create_dense(p, qubo);
+      p->warps = autotune_dense_warps(p);
     } catch (...) {
       delete p;
       throw;

@@ -72,6 +72,20 @@ def test_energy_batch_is_reference_bit_exact(native, orc, ctx):
     assert np.array_equal(native.energy_batch(f, states, ctx=ctx), orc.energy_batch(f, states))
 
 
+def _ks(a, b):
+    """Two-sample KS test on energies compared at the re-score tolerance:
+    values of `a` within REL of a value of `b` take that value, so ground
+    states found by both sides count as the same energy."""
+    a = np.asarray(a, dtype=np.float64).copy()
+    ub = np.unique(np.asarray(b, dtype=np.float64))
+    idx = np.clip(np.searchsorted(ub, a), 1, len(ub) - 1) if len(ub) > 1 else np.zeros(len(a), dtype=int)
+    for cand in (idx - 1, idx):
+        c = ub[np.clip(cand, 0, len(ub) - 1)]
+        close = np.abs(a - c) <= REL * np.abs(c)
+        a[close] = c[close]
+    return stats.ks_2samp(a, b)
+
+
 def _rescore_ok(orc, f, res):
     e = orc.energy_batch(f, res.traj_states)
     np.testing.assert_allclose(res.traj_energies, e, rtol=REL, atol=0)
@@ -113,7 +127,7 @@ def test_energy_distribution_matches_oracle(native, orc, ctx, site_order, accept
     res = native.anneal(f, beta, num_tries=T, sweeps_per_beta=spb, site_order=site_order,
                         acceptance=acceptance, seed=11, ctx=ctx)
     _, e_ref, _ = orc.anneal_free(f, beta, T, spb, seed=99, acceptance=acceptance, site_order=site_order)
-    ks = stats.ks_2samp(res.traj_energies, e_ref)
+    ks = _ks(res.traj_energies, e_ref)
     assert ks.pvalue > 1e-3, (ks, res.traj_energies.mean(), e_ref.mean())
 
 
@@ -204,7 +218,7 @@ def test_sparse_matches_rescore_and_dense_statistics(native, orc, ctx):
     rd = native.anneal(f, beta, num_tries=400, sweeps_per_beta=2, site_order=1, acceptance=1, seed=6, ctx=ctx)
     # Same Markov chain family (sequential sweeps in different site orders):
     # final best-energy distributions agree.
-    ks = stats.ks_2samp(rs.traj_energies, rd.traj_energies)
+    ks = _ks(rs.traj_energies, rd.traj_energies)
     assert ks.pvalue > 1e-3, ks
 
 
@@ -216,7 +230,7 @@ def test_sparse_energy_distribution_matches_oracle(native, orc, ctx):
     # Oracle: sequential sweeps in the same colour-sorted order are not
     # available there; natural order gives the same stationary behaviour.
     _, e_ref, _ = orc.anneal_free(f, beta, 500, 1, seed=8, acceptance=1, site_order=1)
-    ks = stats.ks_2samp(rs.traj_energies, e_ref)
+    ks = _ks(rs.traj_energies, e_ref)
     assert ks.pvalue > 1e-3, ks
 
 
@@ -265,7 +279,7 @@ def test_batched_rescore_and_statistics(native, orc, ctx):
         assert r.max_field_drift < 1e-4
         single = native.anneal(f, beta, num_tries=160, site_order=1, acceptance=1, resync_every=16, seed=77,
                                ctx=ctx)
-        ks = stats.ks_2samp(r.traj_energies, single.traj_energies)
+        ks = _ks(r.traj_energies, single.traj_energies)
         assert ks.pvalue > 1e-3, (f.shape[0], ks)
 
 
