@@ -596,7 +596,7 @@ CONFIG_NAMES = {
 }
 
 
-PROFILE_CASES = ("exhaustive32", "sa-sk1024", "sa-batch48", "sa-chimera")
+PROFILE_CASES = ("exhaustive32", "exhaustive36", "sa-sk1024", "sa-batch48", "sa-chimera")
 
 
 def profile_case(name: str, ctx) -> None:
@@ -605,8 +605,8 @@ def profile_case(name: str, ctx) -> None:
     most, a handful of launches."""
     import torch
     import onesolver_gb300 as osg
-    if name == "exhaustive32":
-        plan = osg.ExhaustivePlan(int_qubo(32, 0), ctx=ctx)
+    if name in ("exhaustive32", "exhaustive36"):
+        plan = osg.ExhaustivePlan(int_qubo(int(name[-2:]), 0), ctx=ctx, max_minimisers=1 << 16)
     elif name == "sa-sk1024":
         plan = osg.AnnealPlan(sk_qubo(1024, 0), osg.geometric_schedule(0.1, 5.0, 10), num_tries=512,
                               acceptance=osg.ACCEPT_PHYSICAL, site_order=osg.SITES_SEQUENTIAL, ctx=ctx)
