@@ -492,9 +492,13 @@ def bench_learned(args, ctx, pg, rank, world):
     return out
 
 
-# DRAM bytes per launch of the dominant kernel, from the ncu captures
-# summarised under profiles/ (null until captured).
-TRAFFIC: dict = {}
+# DRAM bytes (read + write) per launch of the dominant kernel, from one ncu
+# capture (dram__bytes_read.sum + dram__bytes_write.sum) of the n = 36
+# launch. The exhaustive launch moves a constant 2.03 MB (coefficients,
+# per-CTA records and kept states) whatever the number of states. The SA kernels keep their
+# working set on chip for a launch; their DRAM bytes per launch depend on the
+# chunk length, not on the attempts, and are not reported.
+TRAFFIC: dict = {"exhaustive36": 2029056}
 
 
 # ---------------------------------------------------------------------------
