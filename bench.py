@@ -431,6 +431,9 @@ def bench_sa(args, ctx, pg, rank, world, workload):
     return out
 
 
+WARM_BETA_MIN = 2.0  # schedule of the warm-started runs and of their fair-coin control
+
+
 def bench_learned(args, ctx, pg, rank, world):
     import torch
     import onesolver_gb300 as osg
@@ -450,18 +453,25 @@ def bench_learned(args, ctx, pg, rank, world):
         target = osg.anneal(f, osg.geometric_schedule(0.1, 5.0, args.learned_target_sweeps), num_tries=512,
                             site_order=1, acceptance=osg.ACCEPT_PHYSICAL, resync_every=500, seed=99,
                             ctx=ctx).energy
+        net.predict(f)                                                      # warm the kernels once
+        t0 = time.perf_counter()
         prob = net.predict(f)
-        gate = ws.probe_gate(f, prob, beta_min=1.0, ctx=ctx)
+        t_pred = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        gate = ws.probe_gate(f, prob, beta_min=WARM_BETA_MIN, ctx=ctx)
+        t_gate = time.perf_counter() - t0
         plain = ws.time_to_target(f, target, ctx=ctx)                       # config schedule, fair coins
-        cold = ws.time_to_target(f, target, beta_min=1.0, ctx=ctx)          # warm runs' schedule, fair coins
-        warm = ws.time_to_target(f, target, init_prob=prob, beta_min=1.0, ctx=ctx)
-        chosen = warm if gate.use_warm else cold
+        cold = ws.time_to_target(f, target, beta_min=WARM_BETA_MIN, ctx=ctx)  # warm runs' schedule, fair coins
+        warm = ws.time_to_target(f, target, init_prob=prob, beta_min=WARM_BETA_MIN, ctx=ctx)
+        # The warm arm pays for its prediction; the gate's probe runs are reported apart.
+        warm_s = warm.seconds + t_pred if warm.seconds is not None else None
+        chosen_s = warm_s if gate.use_warm else cold.seconds
         rows.append({"seed": 10000 + k, "target": target, "use_warm": bool(gate.use_warm),
-                     "probe_warm": gate.warm_energy, "probe_cold": gate.cold_energy,
+                     "probe_warm": gate.warm_energy, "probe_cold": gate.cold_energy, "gate_s": t_gate,
                      "plain_sweeps": plain.sweeps, "plain_s": plain.seconds,
                      "cold_sweeps": cold.sweeps, "cold_s": cold.seconds,
-                     "warm_sweeps": warm.sweeps, "warm_s": warm.seconds,
-                     "chosen_s": chosen.seconds,
+                     "warm_sweeps": warm.sweeps, "warm_run_s": warm.seconds, "predict_s": t_pred,
+                     "warm_s": warm_s, "chosen_s": chosen_s,
                      "prob_abs_dev": float(np.mean(np.abs(prob - 0.5)))})
     def med(key):
         v = [r[key] for r in rows if r[key] is not None]
@@ -469,18 +479,24 @@ def bench_learned(args, ctx, pg, rank, world):
     succ = lambda key: sum(r[key] is not None for r in rows) / len(rows)
     value = med("chosen_s")
     out = {
-        "metric": "SA time-to-target (within 0.5% of a long plain-SA best), learned warm start with probe gate",
+        "metric": "SA time-to-target (within 0.5% of a long plain-SA best), learned warm start with probe gate "
+                  "(prediction time included, probe runs reported apart)",
         "value": value, "unit": "s", "ms_per_step": None, "dtype": "fp32 fields, bf16 network",
         "higher_is_better": False,
         "config": {"workload": f"SK n=1024 J~N(0,1/n); {args.learned_train} training instances (labels: plain "
                                f"batched SA 64 traj x 500 sweeps); {args.learned_eval} held-out seeds; target = "
                                f"best of plain SA 512 traj x {args.learned_target_sweeps} sweeps; 512 trajectories "
                                "per time-to-target run; plain = config schedule beta 0.1->5.0 from fair coins; the warm "
-                               "start and its control (fair coins) both run beta 1.0->5.0; the probe gate compares "
-                               "those two",
-                   "network": "3 message-passing layers, hidden 64, BF16 mma.sync + FP32"},
+                               f"start and its control (fair coins) both run beta {WARM_BETA_MIN}->5.0; the probe gate "
+                               "compares those two",
+                   "network": "3 message-passing layers, hidden 64, BF16 mma.sync + FP32; node features: diagonal, "
+                              "row sum, anchor spin, FP64 power-iteration low-spectrum vector"},
         "result": {"plain_median_s": med("plain_s"), "cold_schedule_random_median_s": med("cold_s"),
-                   "warm_median_s": med("warm_s"),
+                   "warm_median_s": med("warm_s"), "predict_median_s": med("predict_s"),
+                   "gate_median_s": med("gate_s"),
+                   "speedup_vs_plain": (med("plain_s") / value) if value else None,
+                   "median_sweeps": {"plain": med("plain_sweeps"), "cold": med("cold_sweeps"),
+                                     "warm": med("warm_sweeps")},
                    "network_gain": (med("cold_s") / med("warm_s")) if med("cold_s") and med("warm_s") else None,
                    "plain_success": succ("plain_s"), "cold_success": succ("cold_s"), "warm_success": succ("warm_s"),
                    "gate_uses_warm": sum(r["use_warm"] for r in rows), "instances": rows,

@@ -64,26 +64,23 @@ void launch_rescore(const double *d_f, int n, const uint8_t *d_states, int m,
   OS_CUDA(cudaGetLastError());
 }
 
-constexpr int RESCORE_WARPS = 4;
 constexpr int RESCORE_MAX_WORDS = 64;  // n <= 2048
 
 __global__ void __launch_bounds__(RESCORE_WARPS * 32) energy_rescore_warp_kernel(const double *__restrict__ f, int n,
                                                                                 const uint8_t *__restrict__ states,
                                                                                 int m, double *__restrict__ out) {
-  __shared__ unsigned xw[RESCORE_WARPS][RESCORE_MAX_WORDS];
-  const int w = threadIdx.x >> 5;
-  const int state = blockIdx.x * RESCORE_WARPS + w;
-  if (state >= m) return;
-  const double e = rescore_energy_warp(f, n, states + (size_t)state * n, xw[w]);
-  if ((threadIdx.x & 31) == 0) out[state] = e;
+  __shared__ unsigned xw[RESCORE_MAX_WORDS];
+  __shared__ double red[RESCORE_WARPS];
+  const int state = blockIdx.x;
+  const double e = rescore_energy_block(f, n, states + (size_t)state * n, xw, red);
+  if (threadIdx.x == 0) out[state] = e;
 }
 
 void launch_rescore_warp(const double *d_f, int n, const uint8_t *d_states, int m,
                          double *d_out, cudaStream_t stream) {
   if (m <= 0) return;
   OS_REQUIRE(n <= RESCORE_MAX_WORDS * 32, "warp re-score supports up to %d variables", RESCORE_MAX_WORDS * 32);
-  const int blocks = (int)ceil_div_u64((uint64_t)m, RESCORE_WARPS);
-  energy_rescore_warp_kernel<<<blocks, RESCORE_WARPS * 32, 0, stream>>>(d_f, n, d_states, m, d_out);
+  energy_rescore_warp_kernel<<<m, RESCORE_WARPS * 32, 0, stream>>>(d_f, n, d_states, m, d_out);
   OS_CUDA(cudaGetLastError());
 }
 

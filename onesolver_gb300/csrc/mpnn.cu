@@ -9,17 +9,22 @@
 //
 // Network (H hidden units, L message-passing layers, n spins):
 //   C^      = C / (rms(C) sqrt(n))           off-diagonal couplings, BF16
-//   X       = [1, d_i / s, r_i / s, [i == 0]] node features: diagonal d_i,
-//             row sum r_i of C, scale s = rms(C) sqrt(n); spin 0 is the anchor
+//   X       = [1, d_i / s, r_i / s, [i == 0], u_i] node features: diagonal
+//             d_i, row sum r_i of C, scale s = rms(C) sqrt(n); spin 0 is the
+//             anchor; u = sqrt(n) v sign(v_0), v the unit vector that power
+//             iteration on (sigma I - C / s) reaches in FP64 (spectral_feature):
+//             the low end of the coupling spectrum, which the ground states of
+//             field-free couplings follow (min over s of s^T C s)
 //   H0      = relu(X W_in + b_in)
 //   M_l     = C^ H_{l-1}                      (n x n) x (n x H) BF16 tensor cores
 //   H_l     = relu(H_{l-1} Ws_l + M_l Wm_l + b_l),   l = 1..L
 //   logit   = H_L w_out + b_out,  p = sigmoid(logit)
 //   loss    = mean BCE(p_i, y_i)
 // A QUBO from a field-free Ising model has the global flip symmetry
-// E(x) = E(1 - x) + const; for such instances labels are oriented with
-// y_0 = 1 (the anchor feature tells the network which spin that is) and the
-// prediction is in that orientation. General QUBOs keep their labels as given.
+// E(x) = E(1 - x) + const; for such instances labels are oriented to agree
+// with the spectral feature (sum_i (2 y_i - 1) u_i >= 0; y_0 = 1 on an exact
+// tie), and the prediction is in that orientation. General QUBOs keep their
+// labels as given.
 //
 // The (n x n) x (n x H) products run on the tensor cores with mma.sync
 // m16n8k16 BF16 -> FP32; the small (n x H) x (H x H) products, the weight
@@ -38,7 +43,9 @@
 namespace os {
 namespace mpnn {
 
-constexpr int FEAT = 4;
+constexpr int FEAT = 5;
+constexpr int SPEC_RHO_ITERS = 16;   // power iterations on C^ for its spectral radius
+constexpr int SPEC_ITERS = 96;       // power iterations on (sigma I - C^), sigma = 1.05 rho
 
 // ---------------------------------------------------------------------------
 // C^ (n x n, BF16, row-major) times Hb (n x H, BF16, row-major) -> out
@@ -248,6 +255,40 @@ using namespace os::mpnn;
 
 // One stored instance: scaled couplings (BF16, padded to np x np), features,
 // optional labels.
+// One power-iteration step in FP64, a warp per row: out = C v^ (mode 0) or
+// sigma v^ - C v^ (mode 1, sigma read from the device), v^ = v / sqrt(*norm_in);
+// the squared norm of out accumulates into *norm_out.
+__global__ void __launch_bounds__(256) spec_step_kernel(const double *__restrict__ c, int n,
+                                                        const double *__restrict__ v,
+                                                        const double *__restrict__ norm_in,
+                                                        const double *__restrict__ sigma_p, int mode,
+                                                        double *__restrict__ out, double *__restrict__ norm_out) {
+  const int row = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (row >= n) return;
+  const double inv = *norm_in > 0.0 ? 1.0 / sqrt(*norm_in) : 0.0;
+  const double *cr = c + (size_t)row * n;
+  double acc = 0.0;
+  for (int j = lane; j < n; j += 32) acc += cr[j] * v[j];
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
+  if (lane == 0) {
+    const double y = mode ? (*sigma_p * v[row] - acc) * inv : acc * inv;
+    out[row] = y;
+    atomicAdd(norm_out, y * y);
+  }
+}
+
+// u_i = sqrt(n) v^_i sign(v^_0) into column `col` of the feature matrix.
+__global__ void spec_feature_kernel(const double *__restrict__ v, const double *__restrict__ norm, int n,
+                                    float *__restrict__ x, int col) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double inv = *norm > 0.0 ? 1.0 / sqrt(*norm) : 0.0;
+  const double sg = v[0] < 0.0 ? -1.0 : 1.0;
+  x[(size_t)i * FEAT + col] = (float)(sqrt((double)n) * v[i] * inv * sg);
+}
+
 struct MpnnInstance {
   int n = 0, np = 0;
   DevBuf<__nv_bfloat16> c;
@@ -354,46 +395,152 @@ void backward(os_mpnn *m, MpnnInstance &in, cudaStream_t s) {
   OS_CUDA(cudaGetLastError());
 }
 
-// Stage an instance: scaled BF16 couplings, features, oriented labels.
-std::unique_ptr<MpnnInstance> stage(const os_qubo_dense *q, const char *label, bool orient) {
+// Start vector of the power iterations: positive, uneven, deterministic.
+// Start vector of the power iterations: positive, uneven, deterministic.
+__host__ __device__ inline double spec_start(int i) {
+  return 1.0 + 0.25 * (double)(((uint32_t)i * 2654435761u) >> 24) / 255.0;
+}
+
+// stats[0] += squares of the off-diagonal upper-triangle coefficients,
+// stats[1] += count of non-finite coefficients on or above the diagonal.
+// A warp per row.
+__global__ void __launch_bounds__(256) stage_stats_kernel(const double *__restrict__ f, int n,
+                                                          double *__restrict__ stats) {
+  const int i = blockIdx.x * 8 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+  if (i >= n) return;
+  double ss = 0.0, bad = 0.0;
+  for (int j = i + lane; j < n; j += 32) {
+    const double v = f[(size_t)i * n + j];
+    if (!isfinite(v)) bad += 1.0;
+    else if (j > i) ss += v * v;
+  }
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    ss += __shfl_xor_sync(0xffffffffu, ss, off);
+    bad += __shfl_xor_sync(0xffffffffu, bad, off);
+  }
+  if (lane == 0) {
+    atomicAdd(&stats[0], ss);
+    if (bad > 0.0) atomicAdd(&stats[1], bad);
+  }
+}
+
+// Scaled symmetric couplings C^ = C / s (BF16, np-padded, and FP64) and the
+// node features of row i (a warp per row); s = rms * sqrt(n) from stats[0]
+// over `pairs` coefficients (1 when they are all zero). The start vector of
+// the power iterations goes to v0, its squared norm to *norm0.
+__global__ void __launch_bounds__(256) stage_build_kernel(const double *__restrict__ f, int n, int np, double pairs,
+                                                          const double *__restrict__ stats,
+                                                          __nv_bfloat16 *__restrict__ cb, double *__restrict__ c64,
+                                                          float *__restrict__ x, double *__restrict__ v0,
+                                                          double *__restrict__ norm0) {
+  const int i = blockIdx.x * 8 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+  if (i >= n) return;
+  const double rms = pairs > 0 ? sqrt(stats[0] / pairs) : 0.0;
+  const double scale = rms > 0 ? rms * sqrt((double)n) : 1.0;
+  double rowsum = 0.0;
+  for (int j = lane; j < n; j += 32) {
+    double v = 0.0;
+    if (j != i) v = i < j ? f[(size_t)i * n + j] : f[(size_t)j * n + i];
+    rowsum += v;
+    cb[(size_t)i * np + j] = __float2bfloat16((float)(v / scale));
+    c64[(size_t)i * n + j] = v / scale;
+  }
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) rowsum += __shfl_xor_sync(0xffffffffu, rowsum, off);
+  if (lane == 0) {
+    float *xi = x + (size_t)i * FEAT;
+    xi[0] = 1.f;
+    xi[1] = (float)(f[(size_t)i * n + i] / scale);
+    xi[2] = (float)(rowsum / scale);
+    xi[3] = i == 0 ? 1.f : 0.f;
+    xi[4] = 0.f;
+    const double s0 = spec_start(i);
+    v0[i] = s0;
+    atomicAdd(norm0, s0 * s0);
+  }
+}
+
+// sigma = 1.05 * rho, rho = sqrt(*rho2) (the norm of C^ v^ after the
+// spectral-radius iterations).
+__global__ void spec_sigma_kernel(const double *__restrict__ rho2, double *__restrict__ sigma) {
+  *sigma = 1.05 * sqrt(*rho2);
+}
+
+// Staged instance with the temporaries of staging (freed once the stream
+// has passed them).
+struct StageTmp {
+  DevBuf<double> f, c64, v[3], norms, stats, sigma;
+};
+
+// Stage an instance on `s`: the QUBO goes up once; scale, BF16 and FP64
+// scaled couplings, node features and the spectral feature are computed on
+// the device. The spectral feature (column 4): SPEC_RHO_ITERS power
+// iterations on C^ estimate its spectral radius rho, then SPEC_ITERS
+// iterations on (1.05 rho I - C^) from the same start vector, FP64
+// throughout, no host round trip. With a label the stream is synchronised,
+// the coefficients checked and the label oriented; without one the caller
+// checks `tmp.stats[1]` (non-finite count) after its own synchronisation.
+std::unique_ptr<MpnnInstance> stage(const os_qubo_dense *q, const char *label, bool orient, cudaStream_t s,
+                                    StageTmp &tmp) {
   const int n = q->n;
   OS_REQUIRE(n >= 2 && n <= 8192, "the network takes 2..8192 spins (got %d)", n);
   auto in = std::make_unique<MpnnInstance>();
   in->n = n;
   in->np = (n + 63) / 64 * 64;
-  double ss = 0.0;
-  long long cnt = 0;
-  for (int i = 0; i < n; ++i)
-    for (int j = i + 1; j < n; ++j) {
-      const double v = q->f[(size_t)i * n + j];
-      OS_REQUIRE(std::isfinite(v), "coefficient (%d,%d) is not finite", i, j);
-      ss += v * v;
-      ++cnt;
+  const size_t nn = (size_t)n * n;
+  tmp.f.alloc(nn);
+  OS_CUDA(cudaMemcpyAsync(tmp.f.get(), q->f, sizeof(double) * nn, cudaMemcpyHostToDevice, s));
+  tmp.stats.alloc(2);
+  const int total = SPEC_RHO_ITERS + SPEC_ITERS + 2;
+  tmp.norms.alloc(total);
+  tmp.sigma.alloc(1);
+  OS_CUDA(cudaMemsetAsync(tmp.stats.get(), 0, sizeof(double) * 2, s));
+  OS_CUDA(cudaMemsetAsync(tmp.norms.get(), 0, sizeof(double) * total, s));
+  in->c.alloc((size_t)in->np * in->np);
+  OS_CUDA(cudaMemsetAsync(in->c.get(), 0, sizeof(__nv_bfloat16) * in->c.count, s));
+  tmp.c64.alloc(nn);
+  in->x.alloc((size_t)n * FEAT);
+  for (auto &b : tmp.v) b.alloc(n);
+  const int rows = (n + 7) / 8;
+  stage_stats_kernel<<<rows, 256, 0, s>>>(tmp.f.get(), n, tmp.stats.get());
+  OS_CUDA(cudaGetLastError());
+  stage_build_kernel<<<rows, 256, 0, s>>>(tmp.f.get(), n, in->np, (double)n * (n - 1) / 2, tmp.stats.get(),
+                                          in->c.get(), tmp.c64.get(), in->x.get(), tmp.v[2].get(),
+                                          tmp.norms.get());
+  OS_CUDA(cudaGetLastError());
+  // Power iterations: step k reads v[k & 1] (v[2] = the start vector for
+  // k = 0) with its squared norm in norms[slot0 + k] and writes the next.
+  auto run = [&](int iters, int mode, int slot0) {
+    for (int k = 0; k < iters; ++k) {
+      const double *vin = k == 0 ? tmp.v[2].get() : tmp.v[k & 1].get();
+      spec_step_kernel<<<rows, 256, 0, s>>>(tmp.c64.get(), n, vin, tmp.norms.get() + slot0 + k,
+                                            mode ? tmp.sigma.get() : nullptr, mode,
+                                            tmp.v[(k + 1) & 1].get(), tmp.norms.get() + slot0 + k + 1);
+      OS_CUDA(cudaGetLastError());
     }
-  const double rms = cnt ? std::sqrt(ss / cnt) : 0.0;
-  const double scale = rms > 0 ? rms * std::sqrt((double)n) : 1.0;
-  std::vector<__nv_bfloat16> c((size_t)in->np * in->np, __float2bfloat16(0.f));
-  std::vector<float> x((size_t)n * FEAT);
-  for (int i = 0; i < n; ++i) {
-    double rowsum = 0.0;
-    for (int j = 0; j < n; ++j) {
-      if (i == j) continue;
-      const double v = i < j ? q->f[(size_t)i * n + j] : q->f[(size_t)j * n + i];
-      rowsum += v;
-      c[(size_t)i * in->np + j] = __float2bfloat16((float)(v / scale));
-    }
-    x[(size_t)i * FEAT + 0] = 1.f;
-    x[(size_t)i * FEAT + 1] = (float)(q->f[(size_t)i * n + i] / scale);
-    x[(size_t)i * FEAT + 2] = (float)(rowsum / scale);
-    x[(size_t)i * FEAT + 3] = i == 0 ? 1.f : 0.f;
-  }
-  in->c.alloc(c.size());
-  OS_CUDA(cudaMemcpy(in->c.get(), c.data(), sizeof(__nv_bfloat16) * c.size(), cudaMemcpyHostToDevice));
-  in->x.alloc(x.size());
-  OS_CUDA(cudaMemcpy(in->x.get(), x.data(), sizeof(float) * x.size(), cudaMemcpyHostToDevice));
+    return iters & 1;
+  };
+  run(SPEC_RHO_ITERS, 0, 0);
+  spec_sigma_kernel<<<1, 1, 0, s>>>(tmp.norms.get() + SPEC_RHO_ITERS, tmp.sigma.get());
+  OS_CUDA(cudaGetLastError());
+  const int slot = SPEC_RHO_ITERS + 1;
+  OS_CUDA(cudaMemcpyAsync(tmp.norms.get() + slot, tmp.norms.get(), sizeof(double), cudaMemcpyDeviceToDevice, s));
+  const int last = run(SPEC_ITERS, 1, slot);
+  spec_feature_kernel<<<(n + 255) / 256, 256, 0, s>>>(tmp.v[last].get(), tmp.norms.get() + slot + SPEC_ITERS, n,
+                                                      in->x.get(), 4);
+  OS_CUDA(cudaGetLastError());
   if (label) {
+    std::vector<float> x((size_t)n * FEAT);
+    double bad = 0.0;
+    OS_CUDA(cudaMemcpyAsync(x.data(), in->x.get(), sizeof(float) * x.size(), cudaMemcpyDeviceToHost, s));
+    OS_CUDA(cudaMemcpyAsync(&bad, tmp.stats.get() + 1, sizeof(double), cudaMemcpyDeviceToHost, s));
+    OS_CUDA(cudaStreamSynchronize(s));
+    OS_REQUIRE(bad == 0.0, "the QUBO has non-finite coefficients");
     std::vector<uint8_t> y(n);
-    const bool flip = orient && label[0] == 0;  // orient so that y_0 = 1
+    double agree = 0.0;
+    for (int i = 0; i < n; ++i) agree += (label[i] ? 1.0 : -1.0) * (double)x[(size_t)i * FEAT + 4];
+    const bool flip = orient && (agree != 0.0 ? agree < 0.0 : label[0] == 0);
     for (int i = 0; i < n; ++i) y[i] = (uint8_t)((label[i] != 0) != flip);
     in->y.alloc(n);
     OS_CUDA(cudaMemcpy(in->y.get(), y.data(), n, cudaMemcpyHostToDevice));
@@ -488,7 +635,9 @@ os_status os_mpnn_add_instance(os_mpnn *m, const os_qubo_dense *q, const char *l
   return guard([&] {
     OS_REQUIRE(m && q && q->f, "null argument");
     activate(m->ctx);
-    m->inst.push_back(stage(q, label, m->orient));
+    StageTmp tmp;
+    m->inst.push_back(stage(q, label, m->orient, m->ctx->stream, tmp));
+    OS_CUDA(cudaStreamSynchronize(m->ctx->stream));
     if (index) *index = (int32_t)m->inst.size() - 1;
   });
 }
@@ -574,7 +723,8 @@ os_status os_mpnn_predict(os_mpnn *m, const os_qubo_dense *q, float *prob) {
     OS_REQUIRE(m && q && q->f && prob, "null argument");
     activate(m->ctx);
     cudaStream_t s = m->ctx->stream;
-    auto in = stage(q, nullptr, m->orient);
+    StageTmp tmp;
+    auto in = stage(q, nullptr, m->orient, s, tmp);
     ensure_work(m, in->np);
     forward(m, *in, s);
     const float *HL = m->Hs.get() + (size_t)m->L * in->np * m->H;
@@ -583,7 +733,10 @@ os_status os_mpnn_predict(os_mpnn *m, const os_qubo_dense *q, float *prob) {
                                                     m->prob.get(), nullptr, nullptr);
     OS_CUDA(cudaGetLastError());
     OS_CUDA(cudaMemcpyAsync(prob, m->prob.get(), sizeof(float) * in->n, cudaMemcpyDeviceToHost, s));
+    double bad = 0.0;
+    OS_CUDA(cudaMemcpyAsync(&bad, tmp.stats.get() + 1, sizeof(double), cudaMemcpyDeviceToHost, s));
     OS_CUDA(cudaStreamSynchronize(s));
+    OS_REQUIRE(bad == 0.0, "the QUBO has non-finite coefficients");
   });
 }
 

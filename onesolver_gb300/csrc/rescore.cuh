@@ -48,54 +48,59 @@ __device__ __forceinline__ double rescore_energy_bits(const double *__restrict__
   return e;
 }
 
-// Warp-parallel FP64 energy of one state, called by all 32 lanes of a warp
-// (the result is returned in every lane). The spins are packed into `xw`
-// (ceil(n / 32) words of shared memory private to the warp); lane l then sums
-// F[i][j] over the set pairs i <= j with j = l mod 32, rows in order, and the
-// lanes' partial sums are reduced with shuffles. Same terms as the
-// reference's sum in a different order: coalesced row reads instead of one
-// serial chain, at an FP64 rounding difference of a few ulps of the sum of
-// the absolute terms.
-__device__ __forceinline__ double rescore_energy_warp(const double *__restrict__ f, int n,
-                                                      const uint8_t *__restrict__ x, unsigned *xw) {
-  const int lane = threadIdx.x & 31;
+// Block-parallel FP64 energy of one state, called by all threads of a CTA of
+// RESCORE_WARPS warps (the result is returned in every thread). The spins are
+// packed into `xw` (ceil(n / 32) words of shared memory); warp w takes the
+// set rows i = w, w + RESCORE_WARPS, ... (in set-row order) and its lane l the
+// columns j >= i with j = l mod 32, four row words in flight at a time; the
+// partial sums meet in `red` (RESCORE_WARPS doubles of shared memory). Same
+// terms as the reference's sum in a different order: coalesced row reads
+// instead of one serial chain, at an FP64 rounding difference of a few ulps
+// of the sum of the absolute terms.
+constexpr int RESCORE_WARPS = 8;
+__device__ __forceinline__ double rescore_energy_block(const double *__restrict__ f, int n,
+                                                       const uint8_t *__restrict__ x, unsigned *xw, double *red) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int nw = (n + 31) >> 5;
-  for (int k = 0; k < nw; ++k) {
+  for (int k = warp; k < nw; k += RESCORE_WARPS) {
     const int j = k * 32 + lane;
     const unsigned b = __ballot_sync(0xffffffffu, j < n && x[j]);
     if (lane == 0) xw[k] = b;
   }
-  __syncwarp();
-  double acc0 = 0.0, acc1 = 0.0;
+  __syncthreads();
+  double acc[4] = {0.0, 0.0, 0.0, 0.0};
+  int seen = 0;
   for (int ki = 0; ki < nw; ++ki) {
     unsigned bits = xw[ki];
     while (bits) {
       const int i = ki * 32 + __ffs(bits) - 1;
       bits &= bits - 1;
+      if (seen++ % RESCORE_WARPS != warp) continue;
       const double *row = f + (size_t)i * n + lane;
-      int kj = ki;
-      for (; kj + 1 < nw; kj += 2) {
-        const unsigned w0 = xw[kj], w1 = xw[kj + 1];
-        const int j0 = kj * 32 + lane;
-        if (j0 >= i && ((w0 >> lane) & 1u)) acc0 += row[kj * 32];
-        if (((w1 >> lane) & 1u)) acc1 += row[(kj + 1) * 32];
-      }
-      if (kj < nw) {
-        const int j0 = kj * 32 + lane;
-        if (j0 >= i && ((xw[kj] >> lane) & 1u)) acc0 += row[kj * 32];
+      for (int kj = ki; kj < nw; kj += 4) {
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const int k = kj + u;
+          if (k < nw && ((xw[k] >> lane) & 1u) && k * 32 + lane >= i) acc[u] += row[k * 32];
+        }
       }
     }
   }
-  double acc = acc0 + acc1;
+  double a = (acc[0] + acc[1]) + (acc[2] + acc[3]);
 #pragma unroll
-  for (int off = 16; off > 0; off >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
-  return acc;
+  for (int off = 16; off > 0; off >>= 1) a += __shfl_xor_sync(0xffffffffu, a, off);
+  if (lane == 0) red[warp] = a;
+  __syncthreads();
+  double e = 0.0;
+#pragma unroll
+  for (int w = 0; w < RESCORE_WARPS; ++w) e += red[w];
+  return e;
 }
 
 void launch_rescore(const double *d_f, int n, const uint8_t *d_states, int m,
                     double *d_out, cudaStream_t stream);
 
-// FP64 energies of m states with rescore_energy_warp (one warp per state).
+// FP64 energies of m states with rescore_energy_block (one CTA per state).
 void launch_rescore_warp(const double *d_f, int n, const uint8_t *d_states, int m,
                          double *d_out, cudaStream_t stream);
 

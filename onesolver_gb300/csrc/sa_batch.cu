@@ -308,8 +308,7 @@ void enqueue_batched(os_sa_plan *p, BatchState &B, cudaStream_t s) {
     OS_BATCH_DISPATCH(p->slot_cls, launch_batch_resync, r, s);
     OS_CUDA(cudaGetLastError());
   }
-  const unsigned grid = (unsigned)ceil_div_u64((unsigned long long)B.total_traj, 4);
-  sa_batch_rescore_kernel<<<grid, 128, 0, s>>>(B.inst.get(), B.traj_inst.get(), B.state_off.get(), B.total_traj,
+  sa_batch_rescore_kernel<<<(unsigned)B.total_traj, RESCORE_WARPS * 32, 0, s>>>(B.inst.get(), B.traj_inst.get(), B.state_off.get(), B.total_traj,
                                               p->xbest.get(), p->states.get(), p->e64.get());
   OS_CUDA(cudaGetLastError());
 }

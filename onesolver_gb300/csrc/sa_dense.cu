@@ -16,6 +16,7 @@
 #include "rescore.cuh"
 #include "sa_common.cuh"
 #include "sa_kernels.cuh"
+#include "sa_init.cuh"
 #include "sa_plan.cuh"
 
 namespace os {
@@ -152,28 +153,75 @@ int dense_warps(int traj, int sm_count, bool tiled) {
   return 4;
 }
 
+// Device staging of a dense instance from the matrix as given (already in
+// HBM for the re-score): the same arrays stage_dense builds on the host.
+// c32 row p (slot order) holds the couplings of site slot_site(p) with every
+// site; c64 row i (site order) those of site i; couplings are the upper
+// triangle of f mirrored, the diagonal is zero and padding sites are zero.
+// A warp per row; *bad counts non-finite coefficients on or above the
+// diagonal.
+__global__ void __launch_bounds__(256) stage_dense_kernel(const double *__restrict__ f, int n, int ld,
+                                                          float *__restrict__ c32, double *__restrict__ c64,
+                                                          float *__restrict__ d32, double *__restrict__ d64,
+                                                          int *__restrict__ bad) {
+  const int row = blockIdx.x * 8 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+  if (row >= ld) return;
+  const int site = slot_site(row >> 5, row & 31);  // c32 row `row`
+  int nonfinite = 0;
+  for (int j = lane; j < ld; j += 32) {
+    double a = 0.0, b = 0.0;
+    if (row < n && j < n && j != row) {
+      a = row < j ? f[(size_t)row * n + j] : f[(size_t)j * n + row];
+      if (row < j && !isfinite(a)) ++nonfinite;
+    }
+    if (site < n && j < n && j != site) b = site < j ? f[(size_t)site * n + j] : f[(size_t)j * n + site];
+    c64[(size_t)row * ld + j] = a;
+    c32[(size_t)row * ld + j] = (float)b;
+  }
+  if (lane == 0) {
+    const double d = row < n ? f[(size_t)row * n + row] : 0.0;
+    if (!isfinite(d)) ++nonfinite;
+    d64[row] = d;
+    d32[row] = (float)d;
+  }
+  if (nonfinite) atomicAdd(bad, nonfinite);
+}
+
 void plan_create_dense(os_sa_plan *p, const os_qubo_dense *q) {
   OS_REQUIRE(q && q->f, "null QUBO");
   OS_REQUIRE(q->n >= 1 && q->n <= MAX_DENSE_N, "dense annealing supports 1..%d variables (got %d)",
              MAX_DENSE_N, q->n);
-  DenseHost hst;
-  stage_dense(q, hst);
+  struct {
+    int n, nslots, ld;
+  } hst;
+  hst.n = q->n;
+  hst.nslots = slots_for(q->n);
+  hst.ld = hst.nslots * 32;
   p->n = hst.n;
   p->nslots = hst.nslots;
   p->ld = hst.ld;
   p->slot_cls = slot_class(hst.nslots);
   const size_t T = p->T;
-  p->c32.alloc(hst.c32.size());
-  p->d32.alloc(hst.d32.size());
-  p->c64.alloc(hst.c64.size());
-  p->d64.alloc(hst.d64.size());
-  p->f.alloc(hst.f.size());
-  OS_CUDA(cudaMemcpy(p->c32.get(), hst.c32.data(), sizeof(float) * hst.c32.size(), cudaMemcpyHostToDevice));
-  OS_CUDA(cudaMemcpy(p->d32.get(), hst.d32.data(), sizeof(float) * hst.d32.size(), cudaMemcpyHostToDevice));
-  OS_CUDA(cudaMemcpy(p->c64.get(), hst.c64.data(), sizeof(double) * hst.c64.size(), cudaMemcpyHostToDevice));
-  OS_CUDA(cudaMemcpy(p->d64.get(), hst.d64.data(), sizeof(double) * hst.d64.size(), cudaMemcpyHostToDevice));
-  OS_CUDA(cudaMemcpy(p->f.get(), hst.f.data(), sizeof(double) * hst.f.size(), cudaMemcpyHostToDevice));
+  const size_t ld = hst.ld;
+  p->c32.alloc(ld * ld);
+  p->d32.alloc(ld);
+  p->c64.alloc(ld * ld);
+  p->d64.alloc(ld);
+  p->f.alloc((size_t)hst.n * hst.n);
+  cudaStream_t s = p->ctx->stream;
+  OS_CUDA(cudaMemcpyAsync(p->f.get(), q->f, sizeof(double) * hst.n * hst.n, cudaMemcpyHostToDevice, s));
+  DevBuf<int> bad;
+  bad.alloc(1);
+  OS_CUDA(cudaMemsetAsync(bad.get(), 0, sizeof(int), s));
+  stage_dense_kernel<<<(unsigned)((ld + 7) / 8), 256, 0, s>>>(p->f.get(), hst.n, hst.ld, p->c32.get(), p->c64.get(),
+                                                             p->d32.get(), p->d64.get(), bad.get());
+  OS_CUDA(cudaGetLastError());
+  int nbad = 0;
+  OS_CUDA(cudaMemcpyAsync(&nbad, bad.get(), sizeof(int), cudaMemcpyDeviceToHost, s));
+  OS_CUDA(cudaStreamSynchronize(s));
+  OS_REQUIRE(nbad == 0, "the QUBO has %d non-finite coefficients", nbad);
   p->h.alloc(T * hst.nslots * 32);
+  dense_init_prepare(p, s);
   p->x.alloc(T * 32);
   p->xbest.alloc(T * 32);
   p->e.alloc(T);
@@ -207,6 +255,25 @@ ResyncArgs dense_resync_args(os_sa_plan *p, int init) {
   r.ebest = p->ebest.get();
   r.drift_bits = p->drift.get();
   return r;
+}
+
+InitArgs dense_init_args(os_sa_plan *p) {
+  InitArgs a{};
+  a.n = p->n;
+  a.nslots = p->nslots;
+  a.ld = p->ld;
+  a.traj_offset = 0;
+  a.seed_lo = (uint32_t)p->seed;
+  a.seed_hi = (uint32_t)(p->seed >> 32);
+  a.instance = 0;
+  a.init_prob = p->init_prob.count ? p->init_prob.get() : nullptr;
+  a.d64 = p->d64.get();
+  a.h = p->h.get();
+  a.x = p->x.get();
+  a.xbest = p->xbest.get();
+  a.e = p->e.get();
+  a.ebest = p->ebest.get();
+  return a;
 }
 
 DenseArgs dense_args(os_sa_plan *p) {
@@ -248,7 +315,7 @@ int autotune_dense_warps(os_sa_plan *p) {
   if (hit != p->ctx->dense_warps.end()) return hit->second;
   cudaStream_t s = p->ctx->stream;
   OS_CUDA(cudaMemsetAsync(p->status.get(), 0, sizeof(int), s));
-  dense_resync(dense_resync_args(p, 1), p->slot_cls, 4, s);
+  dense_init_tc(p, dense_init_args(p), s);
   DenseArgs a = dense_args(p);
   a.step_begin = 0;
   a.step_end = std::min(DENSE_PROBE_STEPS, p->steps);
@@ -281,13 +348,11 @@ void execute_dense(os_sa_plan *p) {
   p->launches = 0;
   OS_CUDA(cudaMemsetAsync(p->accepted.get(), 0, sizeof(unsigned long long) * p->T, s));
   OS_CUDA(cudaMemsetAsync(p->drift.get(), 0, sizeof(unsigned long long), s));
-  ResyncArgs r = dense_resync_args(p, 1);
-  dense_resync(r, p->slot_cls, p->warps, s);
-  ++p->launches;
+  ResyncArgs r = dense_resync_args(p, 0);
+  p->launches += dense_init_tc(p, dense_init_args(p), s);
 
   DenseArgs a = dense_args(p);
   OS_CUDA(cudaMemsetAsync(p->status.get(), 0, sizeof(int), s));
-  r.init = 0;
   const int chunk = p->chunk;
   p->sweep_ev_used = 0;
   for (int s0 = 0; s0 < p->steps; s0 += chunk) {

@@ -641,25 +641,22 @@ __device__ __forceinline__ uint8_t spin_of(const unsigned long long *xm, int k) 
   return (uint8_t)((xm[site_lane(k)] >> site_slot(k)) & 1ull);
 }
 
-// Batched best states -> bytes and FP64 re-score (one warp per trajectory,
-// rescore_energy_warp; 128-thread blocks).
-static __global__ void __launch_bounds__(128) sa_batch_rescore_kernel(const BatchInstance *__restrict__ inst,
-                                                                      const int *__restrict__ traj_inst,
-                                                                      const long long *__restrict__ state_off,
-                                                                      long long total,
-                                                                      const unsigned long long *__restrict__ xbest,
-                                                                      uint8_t *__restrict__ states,
-                                                                      double *__restrict__ e64) {
-  __shared__ unsigned xw[4][64];
-  const long long gt = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  const int lane = threadIdx.x & 31;
+// Batched best states -> bytes and FP64 re-score (one CTA of RESCORE_WARPS
+// warps per trajectory, rescore_energy_block).
+static __global__ void __launch_bounds__(RESCORE_WARPS * 32) sa_batch_rescore_kernel(
+    const BatchInstance *__restrict__ inst, const int *__restrict__ traj_inst,
+    const long long *__restrict__ state_off, long long total, const unsigned long long *__restrict__ xbest,
+    uint8_t *__restrict__ states, double *__restrict__ e64) {
+  __shared__ unsigned xw[64];
+  __shared__ double red[RESCORE_WARPS];
+  const long long gt = blockIdx.x;
   if (gt >= total) return;
   const BatchInstance in = inst[traj_inst[gt]];
   uint8_t *out = states + state_off[gt];
-  for (int site = lane; site < in.n; site += 32) out[site] = spin_of(xbest + gt * 32, site);
-  __syncwarp();
-  const double e = rescore_energy_warp(in.f, in.n, out, xw[threadIdx.x >> 5]);
-  if (lane == 0) e64[gt] = e;
+  for (int site = threadIdx.x; site < in.n; site += blockDim.x) out[site] = spin_of(xbest + gt * 32, site);
+  __syncthreads();
+  const double e = rescore_energy_block(in.f, in.n, out, xw, red);
+  if (threadIdx.x == 0) e64[gt] = e;
 }
 
 // Best states as one byte per variable, for the FP64 re-score.

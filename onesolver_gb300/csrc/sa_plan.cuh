@@ -4,6 +4,8 @@
 
 #include <vector>
 
+#include <cuda_bf16.h>
+
 #include "common.cuh"
 
 namespace os {
@@ -56,6 +58,7 @@ struct os_sa_plan {
   os::DevBuf<float> c32, d32, h, e, ebest;
   os::DevBuf<double> c64, d64;
   os::DevBuf<unsigned long long> x, xbest;
+  os::DevBuf<__nv_bfloat16> bsplit, xmat;   // tensor-core initialisation operands
 
   // sparse
   int ncolors = 0, nnz = 0, traj_per_cta = 0, deg_max = 1;

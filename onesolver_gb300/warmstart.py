@@ -74,7 +74,7 @@ class GateResult:
 
 
 def probe_gate(f: np.ndarray, prob: np.ndarray, *, sweeps: int = 50, num_tries: int = 128, seed: int = 5,
-               beta_min: float = 1.0, beta_max: float = 5.0, ctx: Optional[Context] = None) -> GateResult:
+               beta_min: float = 2.0, beta_max: float = 5.0, ctx: Optional[Context] = None) -> GateResult:
     """Short probe anneals with the same schedule, from the predicted
     probabilities and from fair coins; the warm start is kept only if it ends
     lower on average."""
@@ -94,7 +94,8 @@ class TTT:
 
 
 def time_to_target(f: np.ndarray, target: float, *, rel_gap: float = 0.005, init_prob=None,
-                   budgets: Sequence[int] = (50, 100, 200, 400, 800, 1600), num_tries: int = 512,
+                   budgets: Sequence[int] = (25, 35, 50, 70, 100, 140, 200, 280, 400, 800, 1600),
+                   num_tries: int = 512,
                    beta_min: float = 0.1, beta_max: float = 5.0, seed: int = 21,
                    ctx: Optional[Context] = None) -> TTT:
     """Smallest sweep budget whose best energy is within rel_gap of target."""
@@ -104,7 +105,7 @@ def time_to_target(f: np.ndarray, target: float, *, rel_gap: float = 0.005, init
         beta = geometric_schedule(beta_min, beta_max, s)
         t0 = time.perf_counter()
         r = anneal(f, beta, num_tries=num_tries, site_order=1, acceptance=ACCEPT_PHYSICAL, init_prob=init_prob,
-                   resync_every=max(1, s // 2), seed=seed, ctx=ctx)
+                   resync_every=0, seed=seed, ctx=ctx)
         dt = time.perf_counter() - t0
         res.energies[s] = r.energy
         if r.energy <= thr:

@@ -10,7 +10,9 @@ from __future__ import annotations
 
 import numpy as np
 
-FEAT = 4
+FEAT = 5
+SPEC_RHO_ITERS = 16
+SPEC_ITERS = 96
 
 
 def bf16(a):
@@ -34,6 +36,30 @@ def layout(H: int, L: int):
     return off, p + H + 1
 
 
+def spectral(c: np.ndarray) -> np.ndarray:
+    """Feature u of the GPU's spectral_feature (onesolver_gb300/csrc/mpnn.cu):
+    power iterations on C^ for its spectral radius rho, then on
+    (1.05 rho I - C^) from the same start vector, in FP64; u = sqrt(n) v
+    sign(v_0)."""
+    n = c.shape[0]
+    i = np.arange(n, dtype=np.uint64)
+    v0 = 1.0 + 0.25 * (((i * np.uint64(2654435761)) & np.uint64(0xFFFFFFFF)) >> np.uint64(24)).astype(np.float64) / 255.0
+    v = v0 / np.sqrt(np.sum(v0 * v0))
+    nrm = 0.0
+    for _ in range(SPEC_RHO_ITERS):
+        w = c @ v
+        nrm = np.sqrt(np.sum(w * w))
+        v = w / nrm if nrm > 0 else w * 0.0
+    if not nrm > 0:
+        return np.zeros(n)
+    sigma = 1.05 * nrm
+    v = v0 / np.sqrt(np.sum(v0 * v0))
+    for _ in range(SPEC_ITERS):
+        w = sigma * v - c @ v
+        v = w / np.sqrt(np.sum(w * w))
+    return np.sqrt(n) * v * (-1.0 if v[0] < 0 else 1.0)
+
+
 def stage(f: np.ndarray, use_bf16: bool = True):
     """Scaled couplings C^ and node features X, as the GPU stages them."""
     n = f.shape[0]
@@ -50,13 +76,22 @@ def stage(f: np.ndarray, use_bf16: bool = True):
     x[:, 1] = np.diag(f) / scale
     x[:, 2] = rowsum / scale
     x[0, 3] = 1.0
+    x[:, 4] = spectral(c)
     x = x.astype(np.float32).astype(np.float64)
     return c_hat, x
 
 
-def orient_label(label, orient: bool = True):
+def orient_label(label, orient: bool = True, u=None):
+    """Labels in the orientation that agrees with the spectral feature u
+    (sum_i (2 y_i - 1) u_i >= 0), as the GPU orients them; y_0 = 1 decides
+    an exact tie or a missing u."""
     y = np.asarray(label, dtype=np.float64)
-    return 1.0 - y if (orient and y[0] == 0) else y
+    if not orient:
+        return y
+    a = 0.0 if u is None else float(np.sum((2.0 * y - 1.0) * np.asarray(u, dtype=np.float64)))
+    if a != 0.0:
+        return 1.0 - y if a < 0.0 else y
+    return 1.0 - y if y[0] == 0 else y
 
 
 def loss_grad(params: np.ndarray, f: np.ndarray, label, H: int = 64, L: int = 3, use_bf16: bool = True,
@@ -66,7 +101,7 @@ def loss_grad(params: np.ndarray, f: np.ndarray, label, H: int = 64, L: int = 3,
     off, total = layout(H, L)
     n = f.shape[0]
     c, x = stage(f, use_bf16)
-    y = orient_label(label, orient)
+    y = orient_label(label, orient, x[:, 4])
     q = (lambda a: bf16(a)) if use_bf16 else (lambda a: a)
     W_in = P[off["w_in"]:off["w_in"] + FEAT * H].reshape(FEAT, H)
     b_in = P[off["b_in"]:off["b_in"] + H]

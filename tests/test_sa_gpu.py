@@ -106,6 +106,19 @@ def test_returned_states_rescore(native, orc, ctx, n, site_order, acceptance):
     assert res.attempts == 50 * steps
 
 
+@pytest.mark.parametrize("n,T", [(200, 37), (1024, 130)])
+def test_integer_instance_has_zero_field_drift(native, orc, ctx, n, T):
+    """Integer couplings: the tensor-core initial fields (three BF16 terms,
+    FP32 accumulation) and every FP32 field update are exact, so the FP64
+    resyncs find no drift at all; the states re-score like any other."""
+    f = random_int_qubo(n, 7)
+    beta = native.geometric_schedule(0.2, 3.0, 24)
+    res = native.anneal(f, beta, num_tries=T, site_order=1, acceptance=1, resync_every=6, seed=4, ctx=ctx,
+                        traj_states=True)
+    assert res.max_field_drift == 0.0
+    _rescore_ok(orc, f, res)
+
+
 def test_reference_config_n64(native, orc, ctx):
     """N=64 dense FP64 QUBO, N(0,1) entries from seed 0, num-tries=100,
     num-iter=100, geometric beta 0.1 -> 1.0, the reference's semantics
@@ -151,7 +164,8 @@ def test_plan_api_and_launch_count(native, orc, ctx):
     plan.execute()
     r2 = plan.result(traj_states=True)
     assert np.array_equal(r1.traj_energies, r2.traj_energies)  # same seed: deterministic
-    assert plan.launches == 1 + 2 * 5 + 2
+    # initial spins, fields (tensor cores) and energies; 5 x (sweeps, resync); unpack, re-score
+    assert plan.launches == 3 + 2 * 5 + 2
     _rescore_ok(orc, f, r1)
     plan.close()
 
@@ -164,6 +178,14 @@ def test_invalid_parameters(native, ctx):
         native.anneal(f, [1.0], num_tries=0, ctx=ctx)
     with pytest.raises(native.OneSolverError):
         native.anneal(np.zeros((2049, 2049)), [1.0], ctx=ctx)
+    for i, j in ((2, 5), (3, 3)):
+        g = f.copy()
+        g[i, j] = np.nan
+        with pytest.raises(native.OneSolverError, match="non-finite"):
+            native.anneal(g, [1.0], ctx=ctx)
+    g = f.copy()
+    g[6, 1] = np.inf  # below the diagonal: the reference reads the upper triangle only
+    native.anneal(g, [1.0], ctx=ctx)
     with pytest.raises(native.OneSolverError):
         native.sa_verify(f, [1.0], np.zeros((1, 8), np.uint8), np.full((1, 1), 8, np.int32), np.zeros((1, 1)),
                          ctx=ctx)
