@@ -406,6 +406,15 @@ def bench_sa(args, ctx, pg, rank, world, workload):
     e2e_step = max_over_ranks(pg, statistics.mean(e2e_t))
     k_ms = statistics.mean(kern_ms)
     peak = osg.probe_smem_row_peak(ctx)
+    # The FP32-FMA view: n FMAs per attempt, as a branch-free field update
+    # would do them (dense workloads), against the measured FP32 FMA rate.
+    fma_peak = osg.probe_fp32_fma_peak(ctx)
+    if workload == "sa-batch":
+        fmas_per_step = float(T) * 2000 * float((sizes.astype(np.float64) ** 2).sum())
+    elif workload == "sa-chimera":
+        fmas_per_step = None
+    else:
+        fmas_per_step = float(attempts) * n
     acc_rate = res.accepted / max(res.attempts, 1)
     # The result counters cover the last executed step.
     achieved = smem_bytes / (k_ms * 1e-3) / 1e9
@@ -420,6 +429,10 @@ def bench_sa(args, ctx, pg, rank, world, workload):
                      "frac": achieved / peak, "traffic": TRAFFIC.get(workload), "kernel_ms": k_ms,
                      "kernel_attempts_per_s": attempts / (k_ms * 1e-3),
                      "bytes_per_step": smem_bytes,
+                     "fp32_fma_view": None if fmas_per_step is None else {
+                         "achieved_gflops": 2 * fmas_per_step / (k_ms * 1e-3) / 1e9, "peak_gflops": fma_peak,
+                         "frac": 2 * fmas_per_step / (k_ms * 1e-3) / 1e9 / fma_peak,
+                         "note": "n FP32 FMAs per attempt over os_probe_fp32_fma_peak"},
                      "peak_source": "os_probe_smem_row_peak (128-bit shared loads + paired FP32 FMAs) "
                                     "measured in this run"},
         "e2e": {"value": world * attempts / e2e_step, "unit": "attempts/s", "h2d_bytes_per_step": int(h2d),
