@@ -475,11 +475,13 @@ def bench_learned(args, ctx, pg, rank, world):
         t_gate = time.perf_counter() - t0
         plain = ws.time_to_target(f, target, ctx=ctx)                       # config schedule, fair coins
         cold = ws.time_to_target(f, target, beta_min=WARM_BETA_MIN, ctx=ctx)  # warm runs' schedule, fair coins
-        warm = ws.time_to_target(f, target, init_prob=prob, beta_min=WARM_BETA_MIN, ctx=ctx)
+        warm = ws.time_to_target(f, target, init_prob=ws.sharpen(prob, gate.temperature), beta_min=WARM_BETA_MIN,
+                                 ctx=ctx)
         # The warm arm pays for its prediction; the gate's probe runs are reported apart.
         warm_s = warm.seconds + t_pred if warm.seconds is not None else None
         chosen_s = warm_s if gate.use_warm else cold.seconds
         rows.append({"seed": 10000 + k, "target": target, "use_warm": bool(gate.use_warm),
+                     "temperature": gate.temperature,
                      "probe_warm": gate.warm_energy, "probe_cold": gate.cold_energy, "gate_s": t_gate,
                      "plain_sweeps": plain.sweeps, "plain_s": plain.seconds,
                      "cold_sweeps": cold.sweeps, "cold_s": cold.seconds,

@@ -67,8 +67,10 @@ __device__ __forceinline__ uint32_t pack2(__nv_bfloat16 lo, __nv_bfloat16 hi) {
   return r;
 }
 
-// Requires n % 32 == 0 (padded) and H == 64.
-__global__ void __launch_bounds__(128) gemm_ch_kernel(const __nv_bfloat16 *__restrict__ A, int n,
+// Requires n % 32 == 0 (padded) and H == 64. Split K: CTA (x, y) covers rows
+// [64 x, 64 x + 64) and K range [y ks, (y + 1) ks) and writes its partial
+// product to out + y * n * 64 (ks % 32 == 0).
+__global__ void __launch_bounds__(128) gemm_ch_kernel(const __nv_bfloat16 *__restrict__ A, int n, int ks,
                                                       const __nv_bfloat16 *__restrict__ B, float *__restrict__ out) {
   __shared__ __nv_bfloat16 sA[GM][GK + 8];
   __shared__ __nv_bfloat16 sB[GK][GN + 8];
@@ -80,7 +82,9 @@ __global__ void __launch_bounds__(128) gemm_ch_kernel(const __nv_bfloat16 *__res
   for (int j = 0; j < GN / 8; ++j)
 #pragma unroll
     for (int e = 0; e < 4; ++e) acc[j][e] = 0.f;
-  for (int k0 = 0; k0 < n; k0 += GK) {
+  out += (size_t)blockIdx.y * n * GN;
+  const int kb = blockIdx.y * ks;
+  for (int k0 = kb; k0 < kb + ks; k0 += GK) {
     // Stage A (64 x 32) and B (32 x 64): 2048 elements each, 16 per thread.
     for (int i = threadIdx.x; i < GM * GK; i += blockDim.x) {
       const int r = i / GK, c = i % GK;
@@ -124,6 +128,15 @@ __global__ void __launch_bounds__(128) gemm_ch_kernel(const __nv_bfloat16 *__res
       out[(size_t)r_hi * GN + c + 1] = acc[j][3];
     }
   }
+}
+
+// out[i] = sum over the S partial products, in split order.
+__global__ void sum_parts_kernel(const float *__restrict__ part, int S, size_t count, float *__restrict__ out) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= count) return;
+  float v = part[i];
+  for (int y = 1; y < S; ++y) v += part[(size_t)y * count + i];
+  out[i] = v;
 }
 
 // ---------------------------------------------------------------------------
@@ -307,7 +320,7 @@ struct os_mpnn {
   std::vector<std::unique_ptr<MpnnInstance>> inst;
   // work buffers for n up to cap
   int cap = 0;
-  DevBuf<float> X0pre, Hs, pres, M, dH, dZ, dM, prob, dlogit, loss;
+  DevBuf<float> X0pre, Hs, pres, M, dH, dZ, dM, prob, dlogit, loss, gpart;
   DevBuf<__nv_bfloat16> Hb;
 
   size_t off_win() const { return 0; }
@@ -333,7 +346,20 @@ void ensure_work(os_mpnn *m, int np) {
   m->dlogit.alloc(np);
   m->loss.alloc(1);
   m->Hb.alloc(nh);
+  m->gpart.alloc(4 * nh);
   m->cap = np;
+}
+
+// out (np x 64, FP32) = A (np x np, BF16) B (np x 64, BF16) on the tensor
+// cores, K split over S CTAs per row block (np / 64 x S CTAs) and the S
+// partial products summed in order.
+void gemm_ch(os_mpnn *m, const __nv_bfloat16 *A, int np, const __nv_bfloat16 *B, float *out, cudaStream_t s) {
+  const int S = np % 128 == 0 ? 4 : 2;  // np is a multiple of 64: np / S is a multiple of 32
+  gemm_ch_kernel<<<dim3((unsigned)(np / GM), (unsigned)S), 128, 0, s>>>(A, np, np / S, B, m->gpart.get());
+  OS_CUDA(cudaGetLastError());
+  const size_t count = (size_t)np * GN;
+  sum_parts_kernel<<<(unsigned)ceil_div_u64(count, 256), 256, 0, s>>>(m->gpart.get(), S, count, out);
+  OS_CUDA(cudaGetLastError());
 }
 
 // Forward pass of instance `in` (activations kept for the backward pass).
@@ -349,7 +375,7 @@ void forward(os_mpnn *m, MpnnInstance &in, cudaStream_t s) {
     const float *Hprev = m->Hs.get() + (size_t)l * nh;
     float *Ml = m->M.get() + (size_t)l * nh;
     to_bf16_kernel<<<(unsigned)ceil_div_u64(nh, 256), 256, 0, s>>>(Hprev, m->Hb.get(), nh);
-    gemm_ch_kernel<<<(np + GM - 1) / GM, 128, 0, s>>>(in.c.get(), np, m->Hb.get(), Ml);
+    gemm_ch(m, in.c.get(), np, m->Hb.get(), Ml, s);
     const float *Wl = P + m->off_layer(l);
     linear_kernel<<<n, H, 0, s>>>(Hprev, Wl, Ml, Wl + (size_t)H * H, Wl + 2 * (size_t)H * H, n, H, H, 1,
                                   m->pres.get() + (size_t)(l + 1) * nh, m->Hs.get() + (size_t)(l + 1) * nh);
@@ -385,7 +411,7 @@ void backward(os_mpnn *m, MpnnInstance &in, cudaStream_t s) {
     linear_back_kernel<<<n, H, 0, s>>>(m->dZ.get(), Wl, n, H, H, 0, m->dH.get());
     OS_CUDA(cudaMemsetAsync(m->Hb.get(), 0, sizeof(__nv_bfloat16) * nh, s));
     to_bf16_kernel<<<eb, 256, 0, s>>>(m->dM.get(), m->Hb.get(), rh);
-    gemm_ch_kernel<<<(np + GM - 1) / GM, 128, 0, s>>>(in.c.get(), np, m->Hb.get(), m->dZ.get());
+    gemm_ch(m, in.c.get(), np, m->Hb.get(), m->dZ.get(), s);
     add_kernel<<<eb, 256, 0, s>>>(m->dH.get(), m->dZ.get(), rh);
   }
   // Input layer: dZ0 = dH0 * (pre0 > 0); dW_in = X^T dZ0; db_in = sum dZ0.

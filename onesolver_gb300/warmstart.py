@@ -8,8 +8,8 @@ the C ABI):
 2. ``label_states(instances)`` -- the best state plain SA finds on each
    training instance (one batched anneal).
 3. ``WarmStartNet.train`` -- Adam on the oriented labels.
-4. ``probe_gate`` -- a short probe anneal from the predicted probabilities and
-   from fair coins; the warm start is used only when it ends lower.
+4. ``probe_gate`` -- short probe anneals from the predicted probabilities
+   and from fair coins; the warm start is used only when it ends lower.
 5. ``time_to_target`` -- the sweep budget (and wall time) each method needs to
    come within a relative gap of a target energy.
 
@@ -66,24 +66,45 @@ def train_net(instances, labels, *, epochs: int = 20, lr: float = 2e-3, seed: in
     return net, hist
 
 
+def sharpen(prob: np.ndarray, temperature: float) -> np.ndarray:
+    """sigmoid(logit(p) / temperature): the same per-spin preferences, more
+    (temperature < 1) or less decided."""
+    p = np.clip(np.asarray(prob, dtype=np.float64), 1e-6, 1 - 1e-6)
+    return (1.0 / (1.0 + np.exp(-np.log(p / (1 - p)) / temperature))).astype(np.float32)
+
+
 @dataclass
 class GateResult:
     use_warm: bool
-    warm_energy: float
+    warm_energy: float             # mean probe energy of the chosen temperature
     cold_energy: float
+    temperature: float = 1.0       # sharpening of the kept warm start
+    prob: Optional[np.ndarray] = None  # the warm start to use (None: fair coins)
 
 
 def probe_gate(f: np.ndarray, prob: np.ndarray, *, sweeps: int = 50, num_tries: int = 128, seed: int = 5,
-               beta_min: float = 2.0, beta_max: float = 5.0, ctx: Optional[Context] = None) -> GateResult:
+               beta_min: float = 2.0, beta_max: float = 5.0, temperatures: Sequence[float] = (1.0,),
+               ctx: Optional[Context] = None) -> GateResult:
     """Short probe anneals with the same schedule, from the predicted
-    probabilities and from fair coins; the warm start is kept only if it ends
-    lower on average."""
+    probabilities (sharpened by each temperature) and from fair coins; the
+    warm start with the lowest mean probe energy is kept only if it ends
+    lower than fair coins. The default keeps the network's calibrated
+    probabilities: sharper starts end the probe lower on average but, with
+    less spread between trajectories, take longer to the best-of-T target
+    (SK n = 1024: median 85 sweeps at temperature 0.25 against 60 at 1)."""
     beta = geometric_schedule(beta_min, beta_max, sweeps)
-    warm = anneal(f, beta, num_tries=num_tries, site_order=1, acceptance=ACCEPT_PHYSICAL, init_prob=prob,
-                  seed=seed, ctx=ctx)
     cold = anneal(f, beta, num_tries=num_tries, site_order=1, acceptance=ACCEPT_PHYSICAL, seed=seed + 1, ctx=ctx)
-    return GateResult(warm.traj_energies.mean() < cold.traj_energies.mean(), float(warm.traj_energies.mean()),
-                      float(cold.traj_energies.mean()))
+    best = None
+    for tau in temperatures:
+        p = sharpen(prob, tau)
+        warm = anneal(f, beta, num_tries=num_tries, site_order=1, acceptance=ACCEPT_PHYSICAL, init_prob=p,
+                      seed=seed, ctx=ctx)
+        e = float(warm.traj_energies.mean())
+        if best is None or e < best[0]:
+            best = (e, tau, p)
+    e_cold = float(cold.traj_energies.mean())
+    use = best[0] < e_cold
+    return GateResult(use, best[0], e_cold, best[1], best[2] if use else None)
 
 
 @dataclass
