@@ -6,13 +6,22 @@
 // from scratch; here each trajectory needs its FP32 local fields
 // h_j = sum_{i != j} Q_ij x_i before the first sweep. For all trajectories at
 // once that is one product H = X C (T x n by n x n) with X in {0, 1}: it runs
-// on the tensor cores (mma.sync m16n8k16, BF16 operands, FP32 accumulation).
-// The FP32 couplings are split into three BF16 terms, c = c_hi + c_mid + c_lo
-// exactly (8 + 8 + 8 significand bits), and K runs over the three terms, so
-// every product is exact and only the FP32 accumulation rounds: the fields
-// agree with an FP32 sum of the couplings, as the sweeps keep them. The
-// periodic resyncs (FP64, sa_dense_resync_kernel) measure the drift against
-// FP64 fields as before.
+// on the 5th-generation tensor cores (tcgen05.mma kind::f16, BF16 operands,
+// FP32 accumulator in tensor memory). The FP32 couplings are split into three
+// BF16 terms, c = c_hi + c_mid + c_lo exactly (8 + 8 + 8 significand bits),
+// and K runs over the three terms, so every product is exact and only the
+// FP32 accumulation rounds: the fields agree with an FP32 sum of the
+// couplings, as the sweeps keep them. The periodic resyncs (FP64,
+// sa_dense_resync_kernel) measure the drift against FP64 fields as before.
+//
+// CTA tile: 128 trajectories x 128 sites, accumulator in 128 TMEM columns.
+// K advances in chunks of 64: the 4 warps stage the chunk's rows of X and of
+// the split couplings (both K-major) into one of two shared-memory buffers
+// as 8 x 16-byte core matrices, one elected thread issues four K = 16 MMAs
+// and commits them to the buffer's mbarrier, which frees the buffer for the
+// chunk after next. The epilogue reads the accumulator with tcgen05.ld (warp
+// w: trajectories 32 w .. 32 w + 31) and writes the fields straight into the
+// sweep kernels' register layout.
 //
 // The initial spins are the same Philox draws as the FP64 initialisation
 // (stream kStreamInit, one call per group of four slots and lane), so a
@@ -27,41 +36,35 @@
 #include "sa_init.cuh"
 #include "sa_kernels.cuh"
 #include "sa_plan.cuh"
+#include "tc05.cuh"
 
 namespace os {
 namespace sa {
 
 namespace {
 
-constexpr int IM = 64, IN = 64, IK = 32;  // CTA tile of the product
-constexpr int INIT_CHUNK = 8192;          // trajectories per product (bounds X)
+constexpr int IM = 128, IN = 128, IK = 64;  // CTA tile of the product, K chunk
+constexpr int INIT_CHUNK = 8192;            // trajectories per product (bounds X)
+constexpr uint32_t INIT_WAIT_LIMIT = 1u << 26;
+constexpr int INIT_SMEM = 2 * (IM + IN) * IK * 2;  // two stages of A and B chunks (64 KB)
 
-__device__ __forceinline__ void mma_16816(float (&d)[4], const uint32_t (&a)[4], const uint32_t (&b)[2]) {
-  asm volatile(
-      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-      "{%0,%1,%2,%3};\n"
-      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
-      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
-}
-
-__device__ __forceinline__ uint32_t pack(__nv_bfloat16 lo, __nv_bfloat16 hi) {
-  return (uint32_t)__bfloat16_as_ushort(lo) | ((uint32_t)__bfloat16_as_ushort(hi) << 16);
-}
-
-// B = [c_hi; c_mid; c_lo] (3 ld x ld, row k' = term * ld + site i) from the
-// FP64 couplings in site order.
+// Split couplings, K-major for the product: row j (site) holds
+// [c_hi(C_j), c_mid(C_j), c_lo(C_j)] (3 ld wide); C is symmetric, so row j of
+// C is also its column j.
 __global__ void split_kernel(const double *__restrict__ c64, int ld, __nv_bfloat16 *__restrict__ b) {
   const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   const size_t nn = (size_t)ld * ld;
   if (idx >= nn) return;
+  const size_t j = idx / ld, i = idx % ld;
   const float v = (float)c64[idx];
   const __nv_bfloat16 hi = __float2bfloat16(v);
   const float r1 = v - __bfloat162float(hi);
   const __nv_bfloat16 mid = __float2bfloat16(r1);
   const float r2 = r1 - __bfloat162float(mid);
-  b[idx] = hi;
-  b[nn + idx] = mid;
-  b[2 * nn + idx] = __float2bfloat16(r2);
+  __nv_bfloat16 *row = b + j * 3 * ld;
+  row[i] = hi;
+  row[ld + i] = mid;
+  row[2 * ld + i] = __float2bfloat16(r2);
 }
 
 // Initial spins of trajectories [t0, t0 + count): lane masks (x, xbest) and
@@ -92,66 +95,100 @@ __global__ void init_spins_kernel(const InitArgs a, int t0, int count, __nv_bflo
   a.xbest[(size_t)t * 32 + lane] = xl;
 }
 
-// H = X [c_hi; c_mid; c_lo] for trajectories [t0, t0 + count): CTA tile of
-// 64 trajectories x 64 sites, 4 warps of 16 rows, K step 32 over 3 ld. The
-// fields go straight into the sweep kernels' layout ([t][nslots/2][32] FP32
-// pairs, slot s = site_slot(j) in half s & 1 of pair s >> 1, lane site_lane(j)).
+// H = X [c_hi | c_mid | c_lo]^T for trajectories [t0, t0 + count): CTA
+// (x, y) covers trajectories t0 + 128 x .. + 127 and sites 128 y .. + 127.
+// X: xrows x ld (rows past count are zero), Bt: ld x 3 ld. On a bounded wait
+// running out the CTA stops, frees its TMEM and sets *status.
 __global__ void __launch_bounds__(128) init_gemm_kernel(const __nv_bfloat16 *__restrict__ X,
-                                                        const __nv_bfloat16 *__restrict__ B, int ld, int nslots,
-                                                        int t0, int count, float *__restrict__ h) {
-  __shared__ __nv_bfloat16 sA[IM][IK + 8];
-  __shared__ __nv_bfloat16 sB[IK][IN + 8];
+                                                        const __nv_bfloat16 *__restrict__ Bt, int ld, int nslots,
+                                                        int t0, int count, float *__restrict__ h,
+                                                        int *__restrict__ status) {
+  extern __shared__ __align__(1024) unsigned char init_smem[];  // INIT_SMEM bytes
+  // stage b: A chunk at b * 16 KB, B chunk at 32 KB + b * 16 KB
+  auto sA = [&](int b) { return init_smem + b * (IM * IK * 2); };
+  auto sB = [&](int b) { return init_smem + 2 * (IM * IK * 2) + b * (IN * IK * 2); };
+  __shared__ __align__(8) uint64_t bar[2];
+  __shared__ uint32_t tmem_base;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int row0 = blockIdx.x * IM, col0 = blockIdx.y * IN;
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int g = lane >> 2, tg = lane & 3;
-  float acc[IN / 8][4];
-#pragma unroll
-  for (int j = 0; j < IN / 8; ++j)
-#pragma unroll
-    for (int e = 0; e < 4; ++e) acc[j][e] = 0.f;
-  const int K = 3 * ld;
-  for (int k0 = 0; k0 < K; k0 += IK) {
-    const int kx = k0 % ld;  // column of X for this K step (the three terms share X)
-    for (int i = threadIdx.x; i < IM * IK; i += blockDim.x) {
-      const int r = i / IK, c = i % IK;
-      sA[r][c] = X[(size_t)(row0 + r) * ld + kx + c];
-    }
-    for (int i = threadIdx.x; i < IK * IN; i += blockDim.x) {
-      const int r = i / IN, c = i % IN;
-      sB[r][c] = B[(size_t)(k0 + r) * ld + col0 + c];
-    }
-    __syncthreads();
-#pragma unroll
-    for (int kk = 0; kk < IK; kk += 16) {
-      uint32_t a[4];
-      const int ar = warp * 16 + g;
-      a[0] = pack(sA[ar][kk + tg * 2], sA[ar][kk + tg * 2 + 1]);
-      a[1] = pack(sA[ar + 8][kk + tg * 2], sA[ar + 8][kk + tg * 2 + 1]);
-      a[2] = pack(sA[ar][kk + tg * 2 + 8], sA[ar][kk + tg * 2 + 9]);
-      a[3] = pack(sA[ar + 8][kk + tg * 2 + 8], sA[ar + 8][kk + tg * 2 + 9]);
-#pragma unroll
-      for (int j = 0; j < IN / 8; ++j) {
-        uint32_t b[2];
-        const int bc = j * 8 + g;
-        b[0] = pack(sB[kk + tg * 2][bc], sB[kk + tg * 2 + 1][bc]);
-        b[1] = pack(sB[kk + tg * 2 + 8][bc], sB[kk + tg * 2 + 9][bc]);
-        mma_16816(acc[j], a, b);
+  if (warp == 0) {
+    tc05::tmem_alloc(&tmem_base, IN);
+    tc05::tmem_relinquish();
+  }
+  if (tid == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    mbar_fence_init();
+  }
+  tc05::fence_before_sync();
+  __syncthreads();
+  tc05::fence_after_sync();
+  const uint32_t tmem = tmem_base;
+  constexpr uint32_t idesc = tc05::idesc_bf16_f32(IM, IN);
+  const int K = 3 * ld, nchunks = K / IK;
+  bool bad = false;
+  for (int c = 0; c < nchunks; ++c) {
+    const int b = c & 1;
+    if (c >= 2) {  // the MMAs of chunk c - 2 have released buffer b
+      const bool ok = mbar_wait_bounded(&bar[b], (uint32_t)(((c - 2) >> 1) & 1), INIT_WAIT_LIMIT);
+      if (__syncthreads_or(!ok)) {
+        bad = true;
+        break;
       }
     }
-    __syncthreads();
-  }
-  const int rows[2] = {row0 + warp * 16 + g, row0 + warp * 16 + g + 8};
-#pragma unroll
-  for (int j = 0; j < IN / 8; ++j) {
-#pragma unroll
-    for (int e = 0; e < 4; ++e) {
-      const int r = rows[e >> 1];
-      if (r >= count) continue;
-      const int site = col0 + j * 8 + tg * 2 + (e & 1);
-      const int s = site_slot(site), l = site_lane(site);
-      const size_t pair = ((size_t)(t0 + r) * (nslots / 2) + (s >> 1)) * 32 + l;
-      h[2 * pair + (s & 1)] = acc[j][e];
+    const int k0 = c * IK, kx = k0 % ld;
+    for (int p = tid; p < IM * (IK / 8); p += 128) {
+      const int r = p >> 3, kg = p & 7;
+      *reinterpret_cast<uint4 *>(sA(b) + tc05::core_offset(r, kg)) =
+          *reinterpret_cast<const uint4 *>(X + (size_t)(row0 + r) * ld + kx + kg * 8);
+      *reinterpret_cast<uint4 *>(sB(b) + tc05::core_offset(r, kg)) =
+          *reinterpret_cast<const uint4 *>(Bt + (size_t)(col0 + r) * K + k0 + kg * 8);
     }
+    tc05::fence_proxy_async_smem();
+    __syncthreads();
+    if (tid == 0) {
+      tc05::fence_after_sync();
+#pragma unroll
+      for (int kk = 0; kk < IK / 16; ++kk) {
+        const uint64_t ad = tc05::smem_desc(smem_u32(sA(b)) + kk * 256, 128, 1024);
+        const uint64_t bd = tc05::smem_desc(smem_u32(sB(b)) + kk * 256, 128, 1024);
+        tc05::mma_bf16(tmem, ad, bd, idesc, (c > 0 || kk > 0) ? 1u : 0u);
+      }
+      tc05::commit(&bar[b]);
+    }
+  }
+  if (!bad) {  // the last commit covers every MMA issued before it
+    const int c = nchunks - 1;
+    const bool ok = mbar_wait_bounded(&bar[c & 1], (uint32_t)((c >> 1) & 1), INIT_WAIT_LIMIT);
+    bad = __syncthreads_or(!ok);
+  }
+  tc05::fence_after_sync();
+  if (!bad) {
+    const int r = 32 * warp + lane;  // accumulator row = TMEM lane
+    const int t = row0 + r;
+#pragma unroll 1
+    for (int c4 = 0; c4 < IN / 32; ++c4) {
+      uint32_t v[32];
+      tc05::ld_32x32b_x32(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)(c4 * 32), v);
+      tc05::wait_ld();
+      if (t < count) {
+#pragma unroll
+        for (int j = 0; j < 32; ++j) {
+          const int site = col0 + c4 * 32 + j;
+          const int s = site_slot(site), l = site_lane(site);
+          const size_t pair = ((size_t)(t0 + t) * (nslots / 2) + (s >> 1)) * 32 + l;
+          h[2 * pair + (s & 1)] = __uint_as_float(v[j]);
+        }
+      }
+    }
+  } else if (tid == 0 && status) {
+    atomicExch(status, 1);
+  }
+  tc05::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) {
+    tc05::fence_after_sync();
+    tc05::tmem_dealloc(tmem, IN);
   }
 }
 
@@ -181,6 +218,7 @@ __global__ void init_energy_kernel(const InitArgs a, int t0, int count) {
 }  // namespace
 
 void dense_init_prepare(os_sa_plan *p, cudaStream_t s) {
+  OS_CUDA(cudaFuncSetAttribute(init_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, INIT_SMEM));
   const size_t nn = (size_t)p->ld * p->ld;
   p->bsplit.alloc(3 * nn);
   split_kernel<<<(unsigned)ceil_div_u64(nn, 256), 256, 0, s>>>(p->c64.get(), p->ld, p->bsplit.get());
@@ -199,7 +237,8 @@ int dense_init_tc(os_sa_plan *p, const InitArgs &a, cudaStream_t s) {
     init_spins_kernel<<<(count + 3) / 4, 128, 0, s>>>(a, t0, count, p->xmat.get());
     OS_CUDA(cudaGetLastError());
     dim3 grid((unsigned)((count + IM - 1) / IM), (unsigned)(p->ld / IN));
-    init_gemm_kernel<<<grid, 128, 0, s>>>(p->xmat.get(), p->bsplit.get(), p->ld, p->nslots, t0, count, a.h);
+    init_gemm_kernel<<<grid, 128, INIT_SMEM, s>>>(p->xmat.get(), p->bsplit.get(), p->ld, p->nslots, t0, count,
+                                                  a.h, p->status.get());
     OS_CUDA(cudaGetLastError());
     init_energy_kernel<<<(count + 3) / 4, 128, 0, s>>>(a, t0, count);
     OS_CUDA(cudaGetLastError());
