@@ -63,6 +63,7 @@ struct os_sa_plan {
   // sparse
   int ncolors = 0, nnz = 0, traj_per_cta = 0, deg_max = 1;
   os::DevBuf<int> row_ptr, col, color_sites, color_ptr;
+  os::DevBuf<int2> ell;                     // padded neighbour table (site, coupling bits)
   os::DevBuf<float> val32, diag32;
   os::DevBuf<double> val64, diag64;
   os::DevBuf<float> sh;                     // fields [T][n]

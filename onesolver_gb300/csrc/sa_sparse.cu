@@ -39,6 +39,7 @@ struct SparseArgs {
   const int *color_sites;
   const int *color_ptr;
   int ncolors, n, deg_max;
+  const int2 *ell;        // [n][deg_max] (neighbour site, coupling bits); site -1 past a site's degree
   const double *beta;
   int spb, step_begin, step_end, acceptance;
   int T, traj_per_cta;
@@ -51,41 +52,27 @@ struct SparseArgs {
   unsigned long long *accepted;
 };
 
-// Position of the r-th (0-based) set bit of m, r < popc(m): binary search
-// over halves of the remaining window by population count.
-__device__ __forceinline__ int nth_set_bit(unsigned m, int r) {
-  int pos = 0;
+// Neighbour updates of a warp's accepted sites, applied once the colour is
+// decided (no coupler joins two sites of one colour, so the colour's own
+// decisions never read a field these updates touch). `list` holds `cnt`
+// entries (site << 1 | negative); lane l serves neighbour `le` of entry
+// g + lr of each group of `per` entries (lr = l / deg_max, le = l % deg_max),
+// so the shared-memory atomics run with nearly full warps. Four groups per
+// iteration keep their table loads in flight together.
+__device__ __forceinline__ void apply_updates(const uint32_t *__restrict__ list, int cnt, int per, int lr, int le,
+                                              int deg_max, const int2 *__restrict__ ell, float *__restrict__ h) {
+  for (int g = 0; g < cnt; g += 4 * per) {
+    int2 nb[4];
+    uint32_t e[4];
 #pragma unroll
-  for (int w = 16; w > 0; w >>= 1) {
-    const int c = __popc(m & ((1u << w) - 1u));
-    if (r >= c) {
-      r -= c;
-      m >>= w;
-      pos += w;
+    for (int u = 0; u < 4; ++u) {
+      const int r = g + u * per + lr;
+      e[u] = (lr < per && r < cnt) ? list[r] : 0xffffffffu;
+      nb[u] = e[u] != 0xffffffffu ? ell[(size_t)(e[u] >> 1) * deg_max + le] : make_int2(-1, 0);
     }
-  }
-  return pos;
-}
-
-// Warp-cooperative neighbour update. The accepted sites of the warp (mask
-// `M`, lane i holding site k_i with sign sgn_i) are taken `per` at a time;
-// lane l serves edge `le` of the `lr`-th site of each group (lr = l / deg_max,
-// le = l % deg_max, fixed per lane), so the field atomics run with nearly
-// full warps instead of one lane per accepted site.
-__device__ __forceinline__ void spread_updates(unsigned M, int k, float sgn, int per, int lr, int le,
-                                               const int *__restrict__ row_ptr, const int *__restrict__ col,
-                                               const float *__restrict__ val, float *h) {
-  const int cnt = __popc(M);
-  for (int g = 0; g < cnt; g += per) {
-    const int r = g + lr;
-    const bool on = lr < per && r < cnt;
-    const int src = nth_set_bit(M, on ? r : 0);
-    const int ks = __shfl_sync(0xffffffffu, k, src);
-    const float ss = __shfl_sync(0xffffffffu, sgn, src);
-    if (on) {
-      const int r0 = row_ptr[ks];
-      if (le < row_ptr[ks + 1] - r0) atomicAdd(&h[col[r0 + le]], ss * val[r0 + le]);
-    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+      if (nb[u].x >= 0) atomicAdd(&h[nb[u].x], (e[u] & 1u) ? -__int_as_float(nb[u].y) : __int_as_float(nb[u].y));
   }
 }
 
@@ -95,10 +82,11 @@ __global__ void __launch_bounds__(256, 8) sa_sparse_kernel(const __grid_constant
   const int tpt = blockDim.x / R;            // threads per trajectory (multiple of 32)
   const int slot = threadIdx.x / tpt;        // trajectory within the CTA
   const int tid = threadIdx.x % tpt;
-  const int lane = threadIdx.x & 31;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int n = a.n;
   float *h_all = reinterpret_cast<float *>(smem);
   uint8_t *x_all = reinterpret_cast<uint8_t *>(h_all + (size_t)R * n);
+  __shared__ uint32_t s_list[8][128];   // per warp: accepted sites of the colour (<= 4 x 32)
   __shared__ float s_de[8];
   __shared__ double s_e[8], s_eb[8];
   __shared__ int s_improve[8];
@@ -135,13 +123,14 @@ __global__ void __launch_bounds__(256, 8) sa_sparse_kernel(const __grid_constant
         const int mybase = wbase + lane;
         const Philox4 r = philox4x32_10((uint32_t)(c0 + mybase), (uint32_t)step, (uint32_t)t, c3, a.seed_lo,
                                         a.seed_hi);
+        int listed = 0;  // warp-uniform
 #pragma unroll
         for (int m = 0; m < 4; ++m) {
           const int idx = mybase + m * tpt;
           const bool valid = active && idx < cnt;
           int k = 0;
           bool accept = false;
-          float sgn = 0.f;
+          bool neg = false;
           if (valid) {
             k = a.color_sites[c0 + idx];
             const uint32_t w = m == 0 ? r.x : m == 1 ? r.y : m == 2 ? r.z : r.w;
@@ -153,18 +142,25 @@ __global__ void __launch_bounds__(256, 8) sa_sparse_kernel(const __grid_constant
             accept = dE < theta;
             if (accept) {
               x[k] = xk ? 0 : 1;
-              sgn = xk ? -1.f : 1.f;
+              neg = xk;
               de += dE;
               ++acc;
             }
           }
           if (coop) {
             const unsigned M = __ballot_sync(0xffffffffu, accept);
-            if (M) spread_updates(M, k, sgn, per, lr, le, a.row_ptr, a.col, a.val, h);
+            if (accept) s_list[warp][listed + __popc(M & ((1u << lane) - 1u))] = ((uint32_t)k << 1) | (neg ? 1u : 0u);
+            listed += __popc(M);
           } else if (accept) {
+            const float sgn = neg ? -1.f : 1.f;
             const int e1 = a.row_ptr[k + 1];
             for (int e = a.row_ptr[k]; e < e1; ++e) atomicAdd(&h[a.col[e]], sgn * a.val[e]);
           }
+        }
+        if (coop && listed) {
+          __syncwarp();
+          apply_updates(s_list[warp], listed, per, lr, le, a.deg_max, a.ell, h);
+          __syncwarp();
         }
       }
       if (c + 1 < a.ncolors) __syncthreads();
@@ -403,6 +399,18 @@ void plan_create_sparse(os_sa_plan *p, const os_qubo_csr *q) {
   p->deg_max = 0;
   for (int i = 0; i < n; ++i) p->deg_max = std::max(p->deg_max, rp[i + 1] - rp[i]);
   p->deg_max = std::max(p->deg_max, 1);
+  {
+    std::vector<int2> ell((size_t)n * p->deg_max, make_int2(-1, 0));
+    for (int i = 0; i < n; ++i)
+      for (int e = rp[i]; e < rp[i + 1]; ++e) {
+        const float v = (float)vl[e];
+        int bits;
+        std::memcpy(&bits, &v, sizeof bits);
+        ell[(size_t)i * p->deg_max + (e - rp[i])] = make_int2(cl[e], bits);
+      }
+    p->ell.alloc(ell.size());
+    OS_CUDA(cudaMemcpy(p->ell.get(), ell.data(), sizeof(int2) * ell.size(), cudaMemcpyHostToDevice));
+  }
   p->row_ptr.alloc(n + 1);
   p->col.alloc(nnz);
   p->val32.alloc(nnz);
@@ -489,6 +497,7 @@ void execute_sparse(os_sa_plan *p) {
   a.ncolors = p->ncolors;
   a.n = n;
   a.deg_max = p->deg_max;
+  a.ell = p->ell.get();
   a.beta = p->beta.get();
   a.spb = p->spb;
   a.acceptance = p->acceptance;
