@@ -631,7 +631,7 @@ CONFIG_NAMES = {
 }
 
 
-PROFILE_CASES = ("exhaustive32", "exhaustive36", "sa-sk1024", "sa-batch48", "sa-chimera")
+PROFILE_CASES = ("exhaustive32", "exhaustive36", "sa-sk1024", "sa-batch48", "sa-chimera", "mpnn-predict1024")
 
 
 def profile_case(name: str, ctx) -> None:
@@ -653,6 +653,13 @@ def profile_case(name: str, ctx) -> None:
     elif name == "sa-chimera":
         plan = osg.AnnealPlan(chimera_csr(16, 0), osg.linear_schedule(0.1, 2.9, 50), num_tries=1024,
                               acceptance=osg.ACCEPT_PHYSICAL, ctx=ctx)
+    elif name == "mpnn-predict1024":
+        net = osg.WarmStartNet(seed=1, ctx=ctx)
+        p = net.predict(sk_qubo(1024, 3))
+        torch.cuda.synchronize()
+        print(json.dumps({"profile_case": name, "mean_probability": float(p.mean())}))
+        net.close()
+        return
     else:
         raise SystemExit(f"unknown profile case {name}")
     plan.execute()
