@@ -182,6 +182,7 @@ __global__ void __launch_bounds__(128) sa_dense_seq_kernel(const __grid_constant
       const int site = slot_site(s, lane);
       const bool valid = site < a.n;
       const float d = a.diag[site];
+      const unsigned xs0 = __ballot_sync(FULL, (xl >> s) & 1ull);  // spins at the start of the slot
       int p = 0;
       for (;;) {
         const bool xs = (xl >> s) & 1ull;
@@ -191,7 +192,7 @@ __global__ void __launch_bounds__(128) sa_dense_seq_kernel(const __grid_constant
         if (!mask) break;
         const int i = __ffs(mask) - 1;
         const float dEi = __shfl_sync(FULL, dE, i);
-        const bool xi = __shfl_sync(FULL, xs, i);
+        const bool xi = (xs0 >> i) & 1u;
         F.add_row_global(a.c + (size_t)(s * 32 + i) * a.ld + 4 * lane, xi ? -1.f : 1.f, nslots);
         if (lane == i) xl ^= 1ull << s;
         E += dEi;
@@ -351,6 +352,9 @@ __device__ __forceinline__ bool tile_item_impl(const DenseArgs &a, float *tiles,
           const float *tile = tiles + (size_t)half * tile_floats;
           int p = half * TILE_ROWS;
           const int pend = p + TILE_ROWS;
+          // Spins of the slot at the start of the half: a lane's spin only
+          // changes when that lane flips, after which it is past p.
+          const unsigned xs0 = __ballot_sync(FULL, (xl >> s) & 1ull);
           for (;;) {
             const bool xs = (xl >> s) & 1ull;
             const float loc = d + F.get(s);
@@ -359,7 +363,7 @@ __device__ __forceinline__ bool tile_item_impl(const DenseArgs &a, float *tiles,
             if (!mask) break;
             const int i = __ffs(mask) - 1;
             const float dEi = __shfl_sync(FULL, dE, i);
-            const bool xi = __shfl_sync(FULL, xs, i);
+            const bool xi = (xs0 >> i) & 1u;
             F.template add_row<ALL>(tile + (size_t)(i - half * TILE_ROWS) * ld + 4 * lane, xi ? -1.f : 1.f, nslots);
             if (lane == i) xl ^= 1ull << s;
             E += dEi;
