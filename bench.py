@@ -631,7 +631,8 @@ CONFIG_NAMES = {
 }
 
 
-PROFILE_CASES = ("exhaustive32", "exhaustive36", "sa-sk1024", "sa-batch48", "sa-chimera", "mpnn-predict1024")
+PROFILE_CASES = ("exhaustive32", "exhaustive36", "sa-sk1024", "sa-batch48", "sa-batch128x256", "sa-chimera",
+                 "mpnn-predict1024")
 
 
 def profile_case(name: str, ctx) -> None:
@@ -645,6 +646,13 @@ def profile_case(name: str, ctx) -> None:
     elif name == "sa-sk1024":
         plan = osg.AnnealPlan(sk_qubo(1024, 0), osg.geometric_schedule(0.1, 5.0, 10), num_tries=512,
                               acceptance=osg.ACCEPT_PHYSICAL, site_order=osg.SITES_SEQUENTIAL, ctx=ctx)
+    elif name == "sa-batch128x256":
+        # the batched configuration's per-CTA shape (256 trajectories, n ~ U[64, 1024]) on a quarter of
+        # its instances and 8 sweeps: ~1 GB on the device, one short launch
+        rng = np.random.default_rng(0)
+        sizes = rng.integers(64, 1025, size=128)
+        fs = [normal_qubo(int(m), k, scale=1.0 / math.sqrt(m)) for k, m in enumerate(sizes)]
+        plan = osg.BatchedAnnealPlan(fs, osg.geometric_schedule(0.1, 5.0, 8), num_tries=256, ctx=ctx)
     elif name == "sa-batch48":
         rng = np.random.default_rng(0)
         sizes = rng.integers(64, 1025, size=48)
