@@ -242,7 +242,9 @@ typedef struct os_sa_params {
   int32_t acceptance;       /* os_acceptance */
   int32_t site_order;       /* os_site_order */
   int32_t resync_every;     /* steps between FP64 local-field resyncs
-                               (0 = only one check at the end) */
+                               (0 = only one check at the end; -1 = none,
+                               dense plans only: the drift is not measured
+                               and max_field_drift reads -1) */
   const float *init_prob;   /* optional n values: P(x_i = 1) at start (warm
                                start); NULL = fair coin per spin as the
                                reference's bit() (annealing.hpp:91-93) */

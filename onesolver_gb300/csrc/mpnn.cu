@@ -309,6 +309,12 @@ struct MpnnInstance {
   DevBuf<uint8_t> y;   // n (oriented labels) or empty
 };
 
+// Temporaries of staging an instance: the matrix as given, FP64 scaled
+// couplings, power-iteration vectors and norms, coefficient statistics.
+struct StageTmp {
+  DevBuf<double> f, c64, v[3], norms, stats, sigma;
+};
+
 struct os_mpnn {
   os_ctx *ctx = nullptr;
   int H = 64, L = 3;
@@ -322,6 +328,15 @@ struct os_mpnn {
   int cap = 0;
   DevBuf<float> X0pre, Hs, pres, M, dH, dZ, dM, prob, dlogit, loss, gpart;
   DevBuf<__nv_bfloat16> Hb;
+  // prediction: persistent buffers and the captured staging + forward graph
+  // (valid for pgraph_n spins while the work buffers keep capacity pgraph_cap)
+  std::unique_ptr<MpnnInstance> pin;
+  StageTmp ptmp;
+  cudaGraphExec_t pgraph = nullptr;
+  int pgraph_n = 0, pgraph_cap = 0;
+  ~os_mpnn() {
+    if (pgraph) cudaGraphExecDestroy(pgraph);
+  }
 
   size_t off_win() const { return 0; }
   size_t off_bin() const { return (size_t)FEAT * H; }
@@ -493,11 +508,6 @@ __global__ void spec_sigma_kernel(const double *__restrict__ rho2, double *__res
   *sigma = 1.05 * sqrt(*rho2);
 }
 
-// Staged instance with the temporaries of staging (freed once the stream
-// has passed them).
-struct StageTmp {
-  DevBuf<double> f, c64, v[3], norms, stats, sigma;
-};
 
 // Stage an instance on `s`: the QUBO goes up once; scale, BF16 and FP64
 // scaled couplings, node features and the spectral feature are computed on
@@ -507,33 +517,34 @@ struct StageTmp {
 // throughout, no host round trip. With a label the stream is synchronised,
 // the coefficients checked and the label oriented; without one the caller
 // checks `tmp.stats[1]` (non-finite count) after its own synchronisation.
-std::unique_ptr<MpnnInstance> stage(const os_qubo_dense *q, const char *label, bool orient, cudaStream_t s,
-                                    StageTmp &tmp) {
-  const int n = q->n;
-  OS_REQUIRE(n >= 2 && n <= 8192, "the network takes 2..8192 spins (got %d)", n);
-  auto in = std::make_unique<MpnnInstance>();
-  in->n = n;
-  in->np = (n + 63) / 64 * 64;
+// Device buffers of an instance of n spins and of its staging.
+void stage_alloc(MpnnInstance &in, StageTmp &tmp, int n) {
+  in.n = n;
+  in.np = (n + 63) / 64 * 64;
   const size_t nn = (size_t)n * n;
   tmp.f.alloc(nn);
-  OS_CUDA(cudaMemcpyAsync(tmp.f.get(), q->f, sizeof(double) * nn, cudaMemcpyHostToDevice, s));
   tmp.stats.alloc(2);
-  const int total = SPEC_RHO_ITERS + SPEC_ITERS + 2;
-  tmp.norms.alloc(total);
+  tmp.norms.alloc(SPEC_RHO_ITERS + SPEC_ITERS + 2);
   tmp.sigma.alloc(1);
+  in.c.alloc((size_t)in.np * in.np);
+  tmp.c64.alloc(nn);
+  in.x.alloc((size_t)n * FEAT);
+  for (auto &b : tmp.v) b.alloc(n);
+}
+
+// Staging kernels on `s` (tmp.f already holds the matrix): no allocation and
+// no host synchronisation, so the sequence can be captured into a graph.
+void stage_enqueue(MpnnInstance &in, StageTmp &tmp, cudaStream_t s) {
+  const int n = in.n;
+  const int total = SPEC_RHO_ITERS + SPEC_ITERS + 2;
   OS_CUDA(cudaMemsetAsync(tmp.stats.get(), 0, sizeof(double) * 2, s));
   OS_CUDA(cudaMemsetAsync(tmp.norms.get(), 0, sizeof(double) * total, s));
-  in->c.alloc((size_t)in->np * in->np);
-  OS_CUDA(cudaMemsetAsync(in->c.get(), 0, sizeof(__nv_bfloat16) * in->c.count, s));
-  tmp.c64.alloc(nn);
-  in->x.alloc((size_t)n * FEAT);
-  for (auto &b : tmp.v) b.alloc(n);
+  OS_CUDA(cudaMemsetAsync(in.c.get(), 0, sizeof(__nv_bfloat16) * in.c.count, s));
   const int rows = (n + 7) / 8;
   stage_stats_kernel<<<rows, 256, 0, s>>>(tmp.f.get(), n, tmp.stats.get());
   OS_CUDA(cudaGetLastError());
-  stage_build_kernel<<<rows, 256, 0, s>>>(tmp.f.get(), n, in->np, (double)n * (n - 1) / 2, tmp.stats.get(),
-                                          in->c.get(), tmp.c64.get(), in->x.get(), tmp.v[2].get(),
-                                          tmp.norms.get());
+  stage_build_kernel<<<rows, 256, 0, s>>>(tmp.f.get(), n, in.np, (double)n * (n - 1) / 2, tmp.stats.get(),
+                                          in.c.get(), tmp.c64.get(), in.x.get(), tmp.v[2].get(), tmp.norms.get());
   OS_CUDA(cudaGetLastError());
   // Power iterations: step k reads v[k & 1] (v[2] = the start vector for
   // k = 0) with its squared norm in norms[slot0 + k] and writes the next.
@@ -554,8 +565,18 @@ std::unique_ptr<MpnnInstance> stage(const os_qubo_dense *q, const char *label, b
   OS_CUDA(cudaMemcpyAsync(tmp.norms.get() + slot, tmp.norms.get(), sizeof(double), cudaMemcpyDeviceToDevice, s));
   const int last = run(SPEC_ITERS, 1, slot);
   spec_feature_kernel<<<(n + 255) / 256, 256, 0, s>>>(tmp.v[last].get(), tmp.norms.get() + slot + SPEC_ITERS, n,
-                                                      in->x.get(), 4);
+                                                      in.x.get(), 4);
   OS_CUDA(cudaGetLastError());
+}
+
+std::unique_ptr<MpnnInstance> stage(const os_qubo_dense *q, const char *label, bool orient, cudaStream_t s,
+                                    StageTmp &tmp) {
+  const int n = q->n;
+  OS_REQUIRE(n >= 2 && n <= 8192, "the network takes 2..8192 spins (got %d)", n);
+  auto in = std::make_unique<MpnnInstance>();
+  stage_alloc(*in, tmp, n);
+  OS_CUDA(cudaMemcpyAsync(tmp.f.get(), q->f, sizeof(double) * (size_t)n * n, cudaMemcpyHostToDevice, s));
+  stage_enqueue(*in, tmp, s);
   if (label) {
     std::vector<float> x((size_t)n * FEAT);
     double bad = 0.0;
@@ -749,18 +770,52 @@ os_status os_mpnn_predict(os_mpnn *m, const os_qubo_dense *q, float *prob) {
     OS_REQUIRE(m && q && q->f && prob, "null argument");
     activate(m->ctx);
     cudaStream_t s = m->ctx->stream;
-    StageTmp tmp;
-    auto in = stage(q, nullptr, m->orient, s, tmp);
-    ensure_work(m, in->np);
-    forward(m, *in, s);
-    const float *HL = m->Hs.get() + (size_t)m->L * in->np * m->H;
-    float *P = m->param.get();
-    head_kernel<<<(in->n + 255) / 256, 256, 0, s>>>(HL, P + m->off_wout(), P + m->off_bout(), nullptr, in->n, m->H,
+    const int n = q->n;
+    OS_REQUIRE(n >= 2 && n <= 8192, "the network takes 2..8192 spins (got %d)", n);
+    // Persistent buffers and one captured graph per size: the staging, its
+    // 112 power-iteration launches and the forward pass replay as one launch.
+    if (!m->pin || m->pin->n != n) {
+      m->pin = std::make_unique<MpnnInstance>();
+      stage_alloc(*m->pin, m->ptmp, n);
+    }
+    MpnnInstance &in = *m->pin;
+    ensure_work(m, in.np);
+    if (m->pgraph && (m->pgraph_n != n || m->pgraph_cap != m->cap)) {
+      cudaGraphExecDestroy(m->pgraph);
+      m->pgraph = nullptr;
+    }
+    OS_CUDA(cudaMemcpyAsync(m->ptmp.f.get(), q->f, sizeof(double) * (size_t)n * n, cudaMemcpyHostToDevice, s));
+    if (!m->pgraph) {
+      cudaGraph_t g = nullptr;
+      OS_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+      try {
+        stage_enqueue(in, m->ptmp, s);
+        forward(m, in, s);
+        const float *HL = m->Hs.get() + (size_t)m->L * in.np * m->H;
+        float *P = m->param.get();
+        head_kernel<<<(n + 255) / 256, 256, 0, s>>>(HL, P + m->off_wout(), P + m->off_bout(), nullptr, n, m->H,
                                                     m->prob.get(), nullptr, nullptr);
-    OS_CUDA(cudaGetLastError());
-    OS_CUDA(cudaMemcpyAsync(prob, m->prob.get(), sizeof(float) * in->n, cudaMemcpyDeviceToHost, s));
+      } catch (...) {
+        // leave the stream out of capture mode before reporting
+        cudaStreamEndCapture(s, &g);
+        if (g) cudaGraphDestroy(g);
+        (void)cudaGetLastError();
+        throw;
+      }
+      const cudaError_t le = cudaGetLastError();
+      const cudaError_t ce = cudaStreamEndCapture(s, &g);
+      OS_CUDA(le);
+      OS_CUDA(ce);
+      const cudaError_t ie = cudaGraphInstantiate(&m->pgraph, g, 0);
+      cudaGraphDestroy(g);
+      OS_CUDA(ie);
+      m->pgraph_n = n;
+      m->pgraph_cap = m->cap;
+    }
+    OS_CUDA(cudaGraphLaunch(m->pgraph, s));
+    OS_CUDA(cudaMemcpyAsync(prob, m->prob.get(), sizeof(float) * n, cudaMemcpyDeviceToHost, s));
     double bad = 0.0;
-    OS_CUDA(cudaMemcpyAsync(&bad, tmp.stats.get() + 1, sizeof(double), cudaMemcpyDeviceToHost, s));
+    OS_CUDA(cudaMemcpyAsync(&bad, m->ptmp.stats.get() + 1, sizeof(double), cudaMemcpyDeviceToHost, s));
     OS_CUDA(cudaStreamSynchronize(s));
     OS_REQUIRE(bad == 0.0, "the QUBO has non-finite coefficients");
   });

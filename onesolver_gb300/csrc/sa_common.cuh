@@ -82,7 +82,7 @@ inline void check_schedule(const os_sa_params *p) {
              "unknown acceptance rule %d", p->acceptance);
   OS_REQUIRE(p->site_order == OS_SITES_RANDOM || p->site_order == OS_SITES_SEQUENTIAL,
              "unknown site order %d", p->site_order);
-  OS_REQUIRE(p->resync_every >= 0, "resync_every must be >= 0");
+  OS_REQUIRE(p->resync_every >= -1, "resync_every must be >= -1");
   for (int i = 0; i < p->num_iter; ++i)
     OS_REQUIRE(!std::isnan(p->beta[i]), "beta[%d] is NaN", i);
 }

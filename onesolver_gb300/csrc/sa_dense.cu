@@ -362,8 +362,11 @@ void execute_dense(os_sa_plan *p) {
     dense_sweeps(a, p->slot_cls, p->warps, p->sequential, s);
     OS_CUDA(cudaEventRecord(p->event(2 * p->sweep_ev_used + 1), s));
     ++p->sweep_ev_used;
-    dense_resync(r, p->slot_cls, p->warps, s);
-    p->launches += 2;
+    ++p->launches;
+    if (!p->drift_off) {
+      dense_resync(r, p->slot_cls, p->warps, s);
+      ++p->launches;
+    }
   }
   const size_t total = (size_t)p->T * p->n;
   unpack_states_kernel<<<(unsigned)ceil_div_u64(total, 256), 256, 0, s>>>(p->xbest.get(), p->n, p->T,
@@ -389,6 +392,7 @@ void os_sa_plan_common(os_sa_plan *p, os_ctx *ctx, const os_sa_params *prm, int 
   OS_REQUIRE(steps < (1ll << 31), "too many steps (%lld)", steps);
   p->steps = (int)steps;
   p->chunk = prm->resync_every > 0 ? prm->resync_every : p->steps;
+  p->drift_off = prm->resync_every < 0;
   p->seed = prm->seed;
   p->acceptance = prm->acceptance;
   p->sequential = prm->site_order == OS_SITES_SEQUENTIAL;
@@ -432,7 +436,7 @@ os_status os_sa_plan_result(os_sa_plan *p, os_sa_result *res) {
     res->energy = e[best];
     double drift;
     std::memcpy(&drift, &drift_bits, sizeof drift);
-    res->max_field_drift = drift;
+    res->max_field_drift = p->drift_off ? -1.0 : drift;
     res->attempts = (unsigned long long)p->steps * p->attempts_per_step * (unsigned long long)T;
     unsigned long long total = 0;
     for (auto v : acc) total += v;

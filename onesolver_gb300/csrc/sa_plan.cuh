@@ -27,6 +27,7 @@ struct os_sa_plan {
   int launches = 0;
   int warps = 4;
   bool tiled = false;
+  bool drift_off = false;                   // resync_every == -1: no FP64 resync at all
   os::DevBuf<int> status;                   // bounded-wait failures
   // CUDA events around every sweep launch of the last execute (kernel time)
   std::vector<cudaEvent_t> sweep_ev;

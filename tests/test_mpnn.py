@@ -96,3 +96,25 @@ def test_training_learns_and_warm_start_gains(native, orc, ctx):
     cold = native.anneal(f, beta, num_tries=64, site_order=1, acceptance=1, seed=5, ctx=ctx)
     assert warm.traj_energies.mean() < cold.traj_energies.mean()
     net.close()
+
+
+@pytest.mark.gpu
+def test_predict_graph_matches_oracle_and_follows_parameters(native, ctx):
+    """predict() replays one captured graph per size: its probabilities match
+    the oracle's forward pass, repeat exactly, follow a size change and read
+    the current parameters."""
+    net = native.WarmStartNet(seed=3, ctx=ctx)
+    fa, fb = random_normal_qubo(96, 5), random_normal_qubo(160, 6)
+    for f in (fa, fb, fa):
+        p = net.predict(f)
+        _, _, p_ref = mpnn_ref.loss_grad(net.params().astype(np.float64), f, np.zeros(f.shape[0]))
+        np.testing.assert_allclose(p, p_ref, atol=5e-3)
+        assert np.array_equal(net.predict(f), p)
+    p1 = net.predict(fa).astype(np.float64)
+    P = net.params()
+    P[-1] += 1.0  # output bias: every logit moves by +1
+    net.set_params(P)
+    p2 = net.predict(fa).astype(np.float64)
+    logit = lambda q: np.log(q / (1 - q))
+    np.testing.assert_allclose(logit(p2) - logit(p1), 1.0, atol=2e-3)
+    net.close()

@@ -155,6 +155,22 @@ def test_warm_start_bias(native, orc, ctx):
     assert res.energy == e_min
 
 
+def test_no_resync_mode(native, orc, ctx):
+    """resync_every = -1: no FP64 resync at all (drift reported as -1), the
+    same trajectories as with a final resync, states still re-scored."""
+    f = random_normal_qubo(96, 4)
+    beta = native.geometric_schedule(0.2, 3.0, 30)
+    a = native.anneal(f, beta, num_tries=40, site_order=1, acceptance=1, resync_every=-1, seed=9, ctx=ctx,
+                      traj_states=True)
+    b = native.anneal(f, beta, num_tries=40, site_order=1, acceptance=1, resync_every=0, seed=9, ctx=ctx,
+                      traj_states=True)
+    assert a.max_field_drift == -1.0 and b.max_field_drift >= 0.0
+    assert np.array_equal(a.traj_energies, b.traj_energies)
+    _rescore_ok(orc, f, a)
+    with pytest.raises(native.OneSolverError):
+        native.anneal(f, beta, resync_every=-2, ctx=ctx)
+
+
 def test_plan_api_and_launch_count(native, orc, ctx):
     f = random_normal_qubo(96, 1)
     beta = native.linear_schedule(0.1, 2.9, 50)
