@@ -112,6 +112,16 @@ os_status os_model_flatten(const os_model *model, double *out, size_t cap);
  * *len_out gets the full length (excluding NUL). */
 os_status os_model_str(const os_model *model, char *out, size_t cap, size_t *len_out);
 
+/* Ising model in COO text ("i j bias" lines, 1-based variables, i == j a
+ * linear bias, '#' comments) -> QUBO text in the format the reference's
+ * converter writes (benchmarks/annealing/scripts/convert_qbsolv_to_coo.py:
+ * "p qubo 0 N N C", then every (i, j) with i <= j sorted, 0-based):
+ * Q_ii = 2 h_i - 2 sum_j J_ij, Q_ij = 4 J_ij, and *offset = sum J - sum h, so
+ * that E_ising(s) = E_qubo(x) + offset with s = 2x - 1. Call with out = NULL
+ * to learn the length (*len_out). */
+os_status os_ising_to_qubo_text(const char *ising_text, size_t len, char *out, size_t cap, size_t *len_out,
+                                double *offset);
+
 /* qubo::Solution::save (include/model/solution.hpp:58-67): the two-line CSV
  * with the energy at 6 significant digits. */
 os_status os_solution_csv(const char *state, int32_t n, double energy,

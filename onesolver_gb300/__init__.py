@@ -113,6 +113,8 @@ SIGNATURES = {
     "os_model_str": (C.c_int, [_P, C.c_char_p, C.c_size_t, C.POINTER(C.c_size_t)]),
     "os_solution_csv": (C.c_int, [C.c_char_p, C.c_int32, C.c_double, C.c_char_p, C.c_size_t,
                                   C.POINTER(C.c_size_t)]),
+    "os_ising_to_qubo_text": (C.c_int, [C.c_char_p, C.c_size_t, C.c_char_p, C.c_size_t, C.POINTER(C.c_size_t),
+                                        C.POINTER(C.c_double)]),
     "os_exhaustive_run": (C.c_int, [_P, C.POINTER(_QuboDense), C.POINTER(_ExhParams), C.POINTER(_ExhResult)]),
     "os_exhaustive_plan_create": (C.c_int, [_P, C.POINTER(_QuboDense), C.POINTER(_ExhParams), C.POINTER(_P)]),
     "os_exhaustive_plan_execute": (C.c_int, [_P]),
@@ -316,6 +318,18 @@ class Model:
                 self._h = None
         except Exception:
             pass
+
+
+def ising_to_qubo_text(text: str) -> tuple[str, float]:
+    """Ising COO text ("i j bias", 1-based) -> (QUBO text in the reference
+    converter's format, offset) with E_ising(s) = E_qubo(x) + offset."""
+    data = text.encode()
+    need = C.c_size_t(0)
+    off = C.c_double(0.0)
+    _check(lib().os_ising_to_qubo_text(data, len(data), None, 0, C.byref(need), C.byref(off)))
+    buf = C.create_string_buffer(need.value + 1)
+    _check(lib().os_ising_to_qubo_text(data, len(data), buf, need.value + 1, C.byref(need), C.byref(off)))
+    return buf.value.decode(), off.value
 
 
 def solution_csv(state: Sequence[int], energy: float) -> str:

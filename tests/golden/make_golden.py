@@ -14,7 +14,9 @@ instances, so the test suite can run where the reference is absent:
   the flatten layout of tests/qubo_helpers_test.cpp:12-30 and the str() case of
   tests/qubo_test.cpp:42-55;
 * chimera_128_001.qubo / chimera_512_001.qubo -- the QUBO-form Chimera droplet
-  instances of benchmarks/annealing/chimera_droplets_qbsolv, and
+  instances of benchmarks/annealing/chimera_droplets_qbsolv (written by the
+  reference's converter, benchmarks/annealing/scripts/convert_qbsolv_to_coo.py,
+  from chimera_{128,512}_001_ising.txt = benchmarks/annealing/chimera_droplets),
   chimera_golden.json with the published best SA energies
   (benchmarks/annealing/results/*/001.csv) and the tensor-network ground
   states (results/*/groundstates_TN.txt) converted to QUBO energies with
@@ -108,6 +110,9 @@ def chimera(ref: Path) -> dict:
     for size in (128, 512):
         text = (base / "chimera_droplets_qbsolv" / f"{size}power" / "001.txt").read_text()
         (HERE / f"chimera_{size}_001.qubo").write_text(text)
+        # the Ising original the reference's converter turned into the file above
+        ising = (base / "chimera_droplets" / f"{size}power" / "001.txt").read_text()
+        (HERE / f"chimera_{size}_001_ising.txt").write_text(ising)
         tn = (base / "results" / str(size) / "groundstates_TN.txt").read_text().splitlines()[0]
         with open(base / "results" / str(size) / "001.csv") as fh:
             best = min(float(row["energy"]) for row in csv.DictReader(fh))
