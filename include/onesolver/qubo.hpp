@@ -25,7 +25,9 @@
 #define ONESOLVER_QUBO_HPP_
 
 #include <cctype>
+#include <charconv>
 #include <climits>
+#include <cstdint>
 #include <cstdlib>
 #include <istream>
 #include <iterator>
@@ -38,12 +40,19 @@
 
 namespace helpers {
 
-// helpers::hash_pair, include/helpers/hash.hpp:19-35: xor of the element
-// hashes.
+// helpers::hash_pair, include/helpers/hash.hpp:19-35, the hash of the
+// coupler map. The reference xors the element hashes; with std::hash<int>
+// the identity, every coupler (i, j) of a Chimera cell or any banded pattern
+// then falls into a few buckets and the map degrades to linear chains (15 ms
+// to parse a 2,048-spin file). Here the two hashes are mixed (a multiply by
+// the 64-bit golden ratio and a boost-style combine); only the hash values
+// and the map's iteration order differ, not the API.
 struct hash_pair {
   template <class T1, class T2>
   size_t operator()(const std::pair<T1, T2> &p) const {
-    return std::hash<T1>{}(p.first) ^ std::hash<T2>{}(p.second);
+    const uint64_t a = (uint64_t)std::hash<T1>{}(p.first) * 0x9E3779B97F4A7C15ull;
+    const uint64_t b = (uint64_t)std::hash<T2>{}(p.second);
+    return (size_t)(a ^ (b + 0x9E3779B97F4A7C15ull + (a << 6) + (a >> 2)));
   }
 };
 
@@ -277,8 +286,13 @@ public:
       if (r != ed) q = r;  // an exponent without digits is not consumed
     }
     (void)mant;
-    std::string tok(p_, q);
-    out = std::strtod(tok.c_str(), nullptr);
+    // from_chars is correctly rounded like strtod and reads the buffer in
+    // place; it takes no leading '+', which strtod handles.
+    const auto r = std::from_chars(*p_ == '+' ? p_ + 1 : p_, q, out);
+    if (*p_ == '+' || r.ec != std::errc() || r.ptr != q) {
+      std::string tok(p_, q);
+      out = std::strtod(tok.c_str(), nullptr);
+    }
     p_ = q;
     return true;
   }

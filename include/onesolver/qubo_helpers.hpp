@@ -7,16 +7,18 @@
 #ifndef ONESOLVER_QUBO_HELPERS_HPP_
 #define ONESOLVER_QUBO_HELPERS_HPP_
 
+#include <algorithm>
 #include <vector>
 
 #include "onesolver/qubo.hpp"
 
 namespace helpers {
 
+// The same layout written into a caller's buffer of n * n values.
 template <class CoeffType>
-std::vector<CoeffType> flatten_qubo(const qubo::QUBOModel<int, CoeffType> &instance) {
+void flatten_qubo_into(const qubo::QUBOModel<int, CoeffType> &instance, CoeffType *result) {
   const size_t n = instance.get_nodes();
-  std::vector<CoeffType> result(n * n);
+  std::fill(result, result + n * n, CoeffType(0));
   for (auto &kv : instance.linear_terms()) {
     if (kv.first >= 0 && (size_t)kv.first < n)
       result[(size_t)kv.first * n + kv.first] = kv.second;
@@ -29,6 +31,13 @@ std::vector<CoeffType> flatten_qubo(const qubo::QUBOModel<int, CoeffType> &insta
     result[(size_t)i + (size_t)j * n] += kv.second;
     result[(size_t)j + (size_t)i * n] += kv.second;
   }
+}
+
+template <class CoeffType>
+std::vector<CoeffType> flatten_qubo(const qubo::QUBOModel<int, CoeffType> &instance) {
+  const size_t n = instance.get_nodes();
+  std::vector<CoeffType> result(n * n);
+  flatten_qubo_into(instance, result.data());
   return result;
 }
 

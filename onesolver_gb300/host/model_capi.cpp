@@ -83,8 +83,7 @@ os_status os_model_flatten(const os_model *m, double *out, size_t cap) {
     OS_REQUIRE(m && out, "null argument");
     const size_t n = m->model.get_nodes();
     OS_REQUIRE(cap >= n * n, "output holds %zu values, %zu needed", cap, n * n);
-    auto flat = helpers::flatten_qubo(m->model);
-    std::memcpy(out, flat.data(), sizeof(double) * flat.size());
+    helpers::flatten_qubo_into(m->model, out);
   });
 }
 
