@@ -193,49 +193,57 @@ void plan_create_batched(os_sa_plan *p, int num, const os_qubo_dense *qs) {
   B->num = num;
   const int T = p->T;
   // Pack the instances into shared buffers; every matrix starts on a
-  // 128-byte boundary (a multiple of 32 floats / 16 doubles).
-  std::vector<float> c32, d32;
-  std::vector<double> c64, d64, f;
+  // 128-byte boundary (a multiple of 32 floats / 16 doubles). Only the
+  // matrices as given go up; the padded FP32/FP64 arrays are staged on the
+  // device, one kernel per instance.
   std::vector<size_t> oc(num), od(num), of(num);
+  size_t nc = 0, nd = 0, nf = 0;
   int max_slots = 1;
   long long h_total = 0, traj = 0, st_total = 0;
   for (int k = 0; k < num; ++k) {
     OS_REQUIRE(qs[k].f && qs[k].n >= 1, "instance %d is empty", k);
-    DenseHost h;
-    stage_dense(&qs[k], h);
-    OS_REQUIRE(h.ld <= BATCH_MAX_LD, "instance %d has %d variables (batched limit %d)", k, h.n, BATCH_MAX_LD);
-    B->n.push_back(h.n);
-    B->nslots.push_back(h.nslots);
-    B->ld.push_back(h.ld);
-    max_slots = std::max(max_slots, h.nslots);
-    oc[k] = c32.size();
-    c32.insert(c32.end(), h.c32.begin(), h.c32.end());
-    od[k] = d32.size();
-    d32.insert(d32.end(), h.d32.begin(), h.d32.end());
-    c64.insert(c64.end(), h.c64.begin(), h.c64.end());
-    d64.insert(d64.end(), h.d64.begin(), h.d64.end());
-    of[k] = f.size();
-    f.insert(f.end(), h.f.begin(), h.f.end());
-    f.resize((f.size() + 15) / 16 * 16, 0.0);
+    const int n = qs[k].n, nslots = slots_for(n), ld = nslots * 32;
+    OS_REQUIRE(ld <= BATCH_MAX_LD, "instance %d has %d variables (batched limit %d)", k, n, BATCH_MAX_LD);
+    B->n.push_back(n);
+    B->nslots.push_back(nslots);
+    B->ld.push_back(ld);
+    max_slots = std::max(max_slots, nslots);
+    oc[k] = nc;
+    nc += (size_t)ld * ld;
+    od[k] = nd;
+    nd += ld;
+    of[k] = nf;
+    nf += ((size_t)n * n + 15) / 16 * 16;
     B->traj_base.push_back(traj);
     B->h_off.push_back(h_total);
     B->state_off_inst.push_back(st_total);
     traj += T;
-    h_total += (long long)T * h.nslots * 32;
-    st_total += (long long)T * h.n;
+    h_total += (long long)T * nslots * 32;
+    st_total += (long long)T * n;
+  }
+  p->c32.alloc(nc);
+  p->d32.alloc(nd);
+  p->c64.alloc(nc);
+  p->d64.alloc(nd);
+  p->f.alloc(nf);
+  {
+    cudaStream_t s = p->ctx->stream;
+    DevBuf<int> bad;
+    bad.alloc(1);
+    OS_CUDA(cudaMemsetAsync(bad.get(), 0, sizeof(int), s));
+    for (int k = 0; k < num; ++k) {
+      const int n = B->n[k];
+      OS_CUDA(cudaMemcpyAsync(p->f.get() + of[k], qs[k].f, sizeof(double) * n * n, cudaMemcpyHostToDevice, s));
+      stage_dense_device(p->f.get() + of[k], n, B->ld[k], p->c32.get() + oc[k], p->c64.get() + oc[k],
+                         p->d32.get() + od[k], p->d64.get() + od[k], bad.get(), s);
+    }
+    int nbad = 0;
+    OS_CUDA(cudaMemcpyAsync(&nbad, bad.get(), sizeof(int), cudaMemcpyDeviceToHost, s));
+    OS_CUDA(cudaStreamSynchronize(s));
+    OS_REQUIRE(nbad == 0, "the batch has %d non-finite coefficients", nbad);
   }
   B->total_traj = traj;
   p->slot_cls = slot_class(max_slots);
-  p->c32.alloc(c32.size());
-  p->d32.alloc(d32.size());
-  p->c64.alloc(c64.size());
-  p->d64.alloc(d64.size());
-  p->f.alloc(f.size());
-  OS_CUDA(cudaMemcpy(p->c32.get(), c32.data(), sizeof(float) * c32.size(), cudaMemcpyHostToDevice));
-  OS_CUDA(cudaMemcpy(p->d32.get(), d32.data(), sizeof(float) * d32.size(), cudaMemcpyHostToDevice));
-  OS_CUDA(cudaMemcpy(p->c64.get(), c64.data(), sizeof(double) * c64.size(), cudaMemcpyHostToDevice));
-  OS_CUDA(cudaMemcpy(p->d64.get(), d64.data(), sizeof(double) * d64.size(), cudaMemcpyHostToDevice));
-  OS_CUDA(cudaMemcpy(p->f.get(), f.data(), sizeof(double) * f.size(), cudaMemcpyHostToDevice));
   std::vector<BatchInstance> inst(num);
   std::vector<int> tinst(traj);
   std::vector<long long> soff(traj);

@@ -15,21 +15,13 @@ namespace sa {
 
 constexpr int MAX_DENSE_N = 2048;  // 64 field slots per lane
 
-// Dense instance staged for the sweep kernels. Sites are padded to a
-// multiple of 128 (nslots = ld / 32 slots, a multiple of 4); padding sites
-// have zero couplings and never flip. The FP32 coupling rows are stored in
-// slot order: row p = s*32 + l holds the couplings of site
-// ((s >> 2) << 7) + (l << 2) + (s & 3) (the site lane l owns in slot s),
-// columns in site order.
-struct DenseHost {
-  int n = 0, nslots = 0, ld = 0;
-  std::vector<float> c32;    // ld*ld couplings, zero diagonal, rows in slot order
-  std::vector<float> d32;    // ld diagonal (linear) terms
-  std::vector<double> c64;   // ld*ld FP64 couplings, zero diagonal
-  std::vector<double> d64;   // ld
-  std::vector<double> f;     // n*n flattened matrix as given (re-score)
-};
-
+// Dense instances are staged for the sweep kernels on the device
+// (stage_dense_device). Sites are padded to a multiple of 128 (nslots =
+// ld / 32 slots, a multiple of 4); padding sites have zero couplings and
+// never flip. The FP32 coupling rows are stored in slot order: row
+// p = s*32 + l holds the couplings of site ((s >> 2) << 7) + (l << 2) +
+// (s & 3) (the site lane l owns in slot s), columns in site order; the FP64
+// rows (resync) are in site order.
 inline int slots_for(int n) { return (n + 127) / 128 * 4; }
 
 // Power-of-two slot count (>= 4) of the kernel instance that serves nslots.
@@ -39,39 +31,12 @@ inline int slot_class(int nslots) {
   return s;
 }
 
-inline int slot_site_host(int p) {
-  const int s = p >> 5, l = p & 31;
-  return ((s >> 2) << 7) + (l << 2) + (s & 3);
-}
-
-inline void stage_dense(const os_qubo_dense *q, DenseHost &h) {
-  const int n = q->n;
-  h.n = n;
-  h.nslots = slots_for(n);
-  h.ld = h.nslots * 32;
-  const size_t ld = h.ld;
-  h.c32.assign(ld * ld, 0.f);
-  h.c64.assign(ld * ld, 0.0);
-  h.d32.assign(ld, 0.f);
-  h.d64.assign(ld, 0.0);
-  h.f.assign(q->f, q->f + (size_t)n * n);
-  for (int i = 0; i < n; ++i) {
-    const double di = q->f[(size_t)i * n + i];
-    OS_REQUIRE(std::isfinite(di), "coefficient (%d,%d) is not finite", i, i);
-    h.d64[i] = di;
-    h.d32[i] = (float)di;
-    for (int j = i + 1; j < n; ++j) {
-      const double v = q->f[(size_t)i * n + j];
-      OS_REQUIRE(std::isfinite(v), "coefficient (%d,%d) is not finite", i, j);
-      h.c64[i * ld + j] = h.c64[j * ld + i] = v;
-    }
-  }
-  for (size_t p = 0; p < ld; ++p) {
-    const int site = slot_site_host((int)p);
-    if (site >= n) continue;
-    for (int j = 0; j < n; ++j) h.c32[p * ld + j] = (float)h.c64[(size_t)site * ld + j];
-  }
-}
+// Device staging of one dense instance from its matrix as given (d_f, n x n,
+// already in HBM): slot-ordered FP32 rows, site-ordered FP64 rows, both
+// diagonals; *bad accumulates the count of non-finite coefficients on or
+// above the diagonal (sa_dense.cu).
+void stage_dense_device(const double *d_f, int n, int ld, float *c32, double *c64, float *d32, double *d64,
+                        int *bad, cudaStream_t s);
 
 inline void check_schedule(const os_sa_params *p) {
   OS_REQUIRE(p != nullptr, "null parameters");

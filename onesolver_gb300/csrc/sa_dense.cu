@@ -154,7 +154,7 @@ int dense_warps(int traj, int sm_count, bool tiled) {
 }
 
 // Device staging of a dense instance from the matrix as given (already in
-// HBM for the re-score): the same arrays stage_dense builds on the host.
+// HBM for the re-score).
 // c32 row p (slot order) holds the couplings of site slot_site(p) with every
 // site; c64 row i (site order) those of site i; couplings are the upper
 // triangle of f mirrored, the diagonal is zero and padding sites are zero.
@@ -185,6 +185,12 @@ __global__ void __launch_bounds__(256) stage_dense_kernel(const double *__restri
     d32[row] = (float)d;
   }
   if (nonfinite) atomicAdd(bad, nonfinite);
+}
+
+void stage_dense_device(const double *d_f, int n, int ld, float *c32, double *c64, float *d32, double *d64,
+                        int *bad, cudaStream_t s) {
+  stage_dense_kernel<<<(unsigned)((ld + 7) / 8), 256, 0, s>>>(d_f, n, ld, c32, c64, d32, d64, bad);
+  OS_CUDA(cudaGetLastError());
 }
 
 void plan_create_dense(os_sa_plan *p, const os_qubo_dense *q) {
