@@ -23,6 +23,11 @@ Workloads (--workload):
                 --learned-eval held-out seeds the time-to-target (within 0.5%
                 of a long plain-SA best) of the gated warm start vs plain
                 random-init SA, 512 trajectories each. Metric: seconds.
+  pt-droplet    Parallel tempering on the reference's Chimera droplet 512/001
+                (committed fixture): 32 chains x 32 temperatures, 2,000
+                exchange rounds of 5 sweeps. Metric: spin-flip attempts/s;
+                the best energies are reported against the tensor-network
+                ground state and the reference's best published SA energy.
   sa-n64        Dense SA, n = 64, N(0,1) entries (seed 0), 100 trajectories x
                 100 random-site steps, geometric beta 0.1 -> 1.0 with the
                 reference's acceptance rule. Metric: spin-flip attempts/s.
@@ -444,6 +449,59 @@ def bench_sa(args, ctx, pg, rank, world, workload):
     return out
 
 
+def bench_pt(args, ctx, pg, rank, world):
+    """Parallel tempering on the reference's Chimera droplet 512/001 (committed
+    fixture): attempts/s and the best energy against the tensor-network ground
+    state and the reference's best published SA energy."""
+    import torch
+    import onesolver_gb300 as osg
+    g = json.loads((ROOT / "tests" / "golden" / "chimera_golden.json").read_text())["512"]
+    f = osg.Model.load(ROOT / "tests" / "golden" / g["file"]).flatten()
+    csr = osg.Csr.from_dense(f)
+    n = csr.n
+    beta = np.geomspace(0.05, 3.0, 32)
+    chains, rounds, spr, resync = 32, 2000, 5, 200
+    T = chains * len(beta)
+    attempts = T * rounds * spr * n
+    run = lambda: osg.temper_sparse(csr, beta, num_chains=chains, num_rounds=rounds, sweeps_per_round=spr,
+                                    resync_every=resync, seed=1000 * rank + len(dev_ms), ctx=ctx)
+    dev_ms, wall, best = [], [], []
+    for _ in range(args.warmup):
+        run()
+    torch.cuda.synchronize()
+    barrier(pg)
+    sampler = ClockSampler(torch.cuda.current_device())
+    sampler.start()
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        r = run()
+        wall.append(time.perf_counter() - t0)
+        dev_ms.append(r.device_ms)
+        best.append(r.energy)
+    clocks = sampler.stop()
+    barrier(pg)
+    t_dev = max_over_ranks(pg, statistics.mean(dev_ms))
+    t_e2e = max_over_ranks(pg, statistics.mean(wall))
+    launches = 3 + rounds * 2 + rounds // resync + 2
+    h2d = csr.row_ptr.nbytes + csr.col.nbytes + csr.val.nbytes + csr.diag.nbytes + beta.nbytes
+    return {
+        "metric": "parallel-tempering spin-flip attempts/s", "value": world * attempts / (t_dev * 1e-3),
+        "unit": "attempts/s", "ms_per_step": t_dev, "dtype": "fp32",
+        "config": {"workload": f"parallel tempering, Chimera droplet 512/001 (reference fixture), {chains} chains x "
+                               f"{len(beta)} temperatures (beta geometric 0.05->3.0), {rounds} rounds x {spr} sweeps, "
+                               f"FP64 resync every {resync} rounds",
+                   "n": n, "replicas": T, "attempts_per_step": attempts,
+                   "timing": "device_ms: CUDA events around the rounds; e2e: the host-buffer call"},
+        "result": {"best_energy_per_step": best, "tn_ground_qubo": g["tn_ground_qubo"],
+                   "published_best_sa": g["published_best_sa"],
+                   "steps_at_tn_ground": sum(abs(b - g["tn_ground_qubo"]) < 1e-6 for b in best)},
+        "e2e": {"value": world * attempts / t_e2e, "unit": "attempts/s", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(n + 8 * chains + 12 * T + 16 * (len(beta) - 1)), "ms_per_step": t_e2e * 1e3},
+        "gpu_launches": launches * args.steps,
+        "clocks": clocks,
+    }
+
+
 WARM_BETA_MIN = 2.0  # schedule of the warm-started runs and of their fair-coin control
 
 
@@ -592,6 +650,9 @@ def reference_arm(args, world, rank):
         return None
     threads = os.cpu_count() or 1
     w = args.workload
+    if w == "pt-droplet":
+        return {"impl": "reference", "unavailable": "the reference has no parallel tempering "
+                                                    "(benchmarks/annealing/performance.md names it as future work)"}
     vals = []
     sample_desc = ""
     for i in range(args.warmup + args.steps):
@@ -620,6 +681,7 @@ METRICS = {
     "sa-batch": "SA spin-flip attempts/s",
     "sa-n64": "SA spin-flip attempts/s",
     "sa-learned": "SA time-to-target, learned warm start vs plain",
+    "pt-droplet": "parallel-tempering spin-flip attempts/s",
 }
 CONFIG_NAMES = {
     "exhaustive36": "exhaustive search, dense QUBO n=36, integer Q_ij ~ U{-8..8} (seed 0), 2^36 states",
@@ -628,6 +690,7 @@ CONFIG_NAMES = {
     "sa-batch": "batched dense SA, 512 instances n~U[64,1024], 256 trajectories x 2,000 sweeps",
     "sa-n64": "dense SA, n=64, 100 trajectories x 100 steps (reference CLI defaults)",
     "sa-learned": "SK n=1024 learned warm start, time-to-target",
+    "pt-droplet": "parallel tempering, Chimera droplet 512/001, 32 chains x 32 temperatures x 10,000 sweeps",
 }
 
 
@@ -711,7 +774,7 @@ def main():
         return
     if args.steps <= 0:
         args.steps = {"exhaustive36": 50, "sa-chimera": 10, "sa-sk": 5, "sa-batch": 3, "sa-n64": 50,
-                      "sa-learned": 1}[args.workload]
+                      "sa-learned": 1, "pt-droplet": 5}[args.workload]
     args.warmup = max(args.warmup, 3)
 
     world, rank, local, pg = dist_setup(args.gpus)
@@ -736,6 +799,8 @@ def main():
         out = bench_exhaustive(args, ctx, pg, rank, world)
     elif args.workload == "sa-learned":
         out = bench_learned(args, ctx, pg, rank, world)
+    elif args.workload == "pt-droplet":
+        out = bench_pt(args, ctx, pg, rank, world)
     else:
         out = bench_sa(args, ctx, pg, rank, world, args.workload)
 
@@ -751,7 +816,7 @@ def main():
                       "e2e": r["e2e"]["value"], "result": r["result"], "gpu_launches": r["gpu_launches"]}
         out["secondary"] = sec
 
-    if rank == 0 and world == 1 and args.cpu_baseline and args.workload != "sa-learned":
+    if rank == 0 and world == 1 and args.cpu_baseline and args.workload not in ("sa-learned", "pt-droplet"):
         threads = os.cpu_count() or 1
         if args.workload == "exhaustive36":
             rate, sample, dt = cpu_exhaustive_rate(int_qubo(36, 0), 15.0, threads)

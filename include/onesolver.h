@@ -363,6 +363,75 @@ int32_t os_sa_plan_launches(const os_sa_plan *plan);
 os_status os_sa_plan_kernel_ms(os_sa_plan *plan, float *ms);
 void os_sa_plan_destroy(os_sa_plan *plan);
 
+/* ------------------------------------------------------------------------ */
+/* Parallel tempering (replica exchange)                                    */
+/* ------------------------------------------------------------------------ */
+
+/* No reference counterpart: the reference's annealing benchmark recommends
+ * parallel tempering as the next solver after plain annealing
+ * (benchmarks/annealing/performance.md:52-59), whose Chimera runs never reach
+ * the tensor-network ground states (benchmarks/annealing/README:20-21).
+ *
+ * num_chains independent chains of num_temps replicas each. Replica
+ * t = chain * num_temps + r starts at temperature index r from fair-coin
+ * spins and keeps its spins; only temperature labels move. A round is
+ * sweeps_per_round colour-parallel sweeps of every replica at its own
+ * inverse temperature (physical rule exp(-beta dE) > u, FP32 local fields),
+ * then one exchange attempt for every adjacent pair (k, k+1) with
+ * k = round mod 2, k + 2, ... in every chain, accepted when
+ * ln u < (beta[k+1] - beta[k]) * (E_cold - E_hot) with E_hot / E_cold the
+ * tracked energies of the replicas at k / k+1 and u a Philox draw per
+ * (pair, round, chain). */
+typedef struct os_pt_params {
+  const double *beta;        /* num_temps inverse temperatures (host),
+                                finite, >= 0, non-decreasing */
+  int32_t num_temps;         /* replicas per chain, >= 1 */
+  uint32_t num_chains;       /* independent chains, >= 1 */
+  int32_t num_rounds;        /* exchange rounds, >= 1 */
+  int32_t sweeps_per_round;  /* sweeps of every replica per round, >= 1 */
+  uint64_t seed;             /* Philox key (sweeps, initial spins, exchanges) */
+  int32_t resync_every;      /* rounds between FP64 local-field resyncs
+                                (0 = one check at the end) */
+} os_pt_params;
+
+typedef struct os_pt_result {
+  char *state;               /* [n] best state any replica visited */
+  double energy;             /* its FP64 energy (reference energy function) */
+  double *chain_energies;    /* optional [num_chains]: best FP64 energy of
+                                each chain */
+  int32_t *final_temps;      /* optional [num_chains * num_temps]:
+                                temperature index of each replica at the end */
+  double *final_energies;    /* optional [num_chains * num_temps]: FP64
+                                energy of each replica's final state */
+  char *final_states;        /* optional [num_chains * num_temps * n] */
+  uint64_t *swaps_accepted;  /* optional [num_temps - 1]: accepted exchanges
+                                of each adjacent pair, summed over chains */
+  uint64_t *swaps_attempted; /* optional [num_temps - 1] */
+  double max_field_drift;    /* max |h_fp32 - h_fp64| over resyncs */
+  uint64_t attempts;         /* spin-flip attempts performed */
+  uint64_t accepted;         /* accepted flips */
+  double device_ms;          /* device time of the rounds (sweeps, exchanges,
+                                resyncs), CUDA events on the context's stream */
+} os_pt_result;
+
+/* Parallel tempering on a sparse QUBO (CSR as for os_sa_run_sparse), with
+ * the sparse annealing kernel as the sweep; host buffers in and out. At most
+ * 65535 replicas (num_chains * num_temps). */
+os_status os_pt_run_sparse(os_ctx *ctx, const os_qubo_csr *qubo,
+                           const os_pt_params *params, os_pt_result *result);
+
+/* Exchange-only replay for verification: runs the exchange step of
+ * os_pt_run_sparse on the GPU for rounds round0 .. round0 + num_rounds - 1
+ * with every replica's energy held at energies[t] (no sweeps). temps
+ * (num_chains * num_temps, in/out) gives each replica's temperature index
+ * and must be a permutation of 0..num_temps-1 within every chain;
+ * swaps_accepted (optional, num_temps - 1) receives the accepted exchanges
+ * per pair. The same Philox draws as os_pt_run_sparse with that seed. */
+os_status os_pt_exchange_replay(os_ctx *ctx, uint32_t num_chains, int32_t num_temps,
+                                const double *beta, const double *energies,
+                                uint64_t seed, int32_t round0, int32_t num_rounds,
+                                int32_t *temps, uint64_t *swaps_accepted);
+
 /* Philox4x32-10 of the device generator, evaluated on the GPU for `count`
  * consecutive counters starting at ctr (ctr[0] incremented); out receives
  * 4*count words. For checking the generator against its published

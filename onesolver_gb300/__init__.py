@@ -88,6 +88,20 @@ class _SaResult(C.Structure):
                 ("accepted", C.c_uint64)]
 
 
+class _PtParams(C.Structure):
+    _fields_ = [("beta", C.POINTER(C.c_double)), ("num_temps", C.c_int32), ("num_chains", C.c_uint32),
+                ("num_rounds", C.c_int32), ("sweeps_per_round", C.c_int32), ("seed", C.c_uint64),
+                ("resync_every", C.c_int32)]
+
+
+class _PtResult(C.Structure):
+    _fields_ = [("state", C.c_char_p), ("energy", C.c_double), ("chain_energies", C.POINTER(C.c_double)),
+                ("final_temps", C.POINTER(C.c_int32)), ("final_energies", C.POINTER(C.c_double)),
+                ("final_states", C.c_char_p), ("swaps_accepted", C.POINTER(C.c_uint64)),
+                ("swaps_attempted", C.POINTER(C.c_uint64)), ("max_field_drift", C.c_double),
+                ("attempts", C.c_uint64), ("accepted", C.c_uint64), ("device_ms", C.c_double)]
+
+
 _lib: Optional[C.CDLL] = None
 
 # Every symbol of include/onesolver.h with (restype, argtypes).
@@ -144,6 +158,10 @@ SIGNATURES = {
     "os_sa_plan_result_batched": (C.c_int, [_P, C.POINTER(_SaResult)]),
     "os_sa_plan_tuned_warps": (C.c_int32, [_P]),
     "os_sa_plan_kernel_ms": (C.c_int, [_P, C.POINTER(C.c_float)]),
+    "os_pt_run_sparse": (C.c_int, [_P, C.POINTER(_QuboCsr), C.POINTER(_PtParams), C.POINTER(_PtResult)]),
+    "os_pt_exchange_replay": (C.c_int, [_P, C.c_uint32, C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                        C.c_uint64, C.c_int32, C.c_int32, C.POINTER(C.c_int32),
+                                        C.POINTER(C.c_uint64)]),
     "os_philox_sample": (C.c_int, [_P, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.c_int32,
                                    C.POINTER(C.c_uint32)]),
     "os_mpnn_create": (C.c_int, [_P, C.c_int32, C.c_int32, C.c_int32, C.c_uint64, C.POINTER(_P)]),
@@ -635,6 +653,77 @@ class AnnealPlan:
             self.close()
         except Exception:
             pass
+
+
+@dataclass
+class TemperResult:
+    state: np.ndarray            # uint8[n], best state any replica visited
+    energy: float                # its FP64 energy (reference energy function)
+    chain_energies: np.ndarray   # float64[num_chains], best per chain
+    final_temps: np.ndarray      # int32[num_chains, num_temps], temperature index of each replica
+    final_energies: np.ndarray   # float64[num_chains, num_temps], FP64 energy of each final state
+    final_states: Optional[np.ndarray]
+    swaps_accepted: np.ndarray   # uint64[num_temps - 1]
+    swaps_attempted: np.ndarray  # uint64[num_temps - 1]
+    max_field_drift: float
+    attempts: int
+    accepted: int
+    device_ms: float
+
+
+def temper_sparse(csr: Csr, beta: Sequence[float], *, num_chains: int = 32, num_rounds: int = 100,
+                  sweeps_per_round: int = 10, seed: int = 1234, resync_every: int = 0,
+                  ctx: Optional[Context] = None, final_states: bool = False) -> TemperResult:
+    """Parallel tempering on a sparse QUBO: num_chains chains of len(beta)
+    replicas, sweeps_per_round colour-parallel sweeps per round at each
+    replica's inverse temperature, then one even/odd round of adjacent
+    exchanges. No reference counterpart (its annealing benchmark names
+    parallel tempering as the next solver, benchmarks/annealing/performance.md:52-59)."""
+    ctx = ctx or default_context()
+    q = csr._c()
+    b = np.ascontiguousarray(beta, dtype=np.float64)
+    nt, n = len(b), csr.n
+    prm = _PtParams(_dptr(b), nt, num_chains, num_rounds, sweeps_per_round, seed, resync_every)
+    T = num_chains * nt
+    state = C.create_string_buffer(n)
+    ce = np.zeros(num_chains, dtype=np.float64)
+    ft = np.zeros(T, dtype=np.int32)
+    fe = np.zeros(T, dtype=np.float64)
+    sa = np.zeros(max(nt - 1, 1), dtype=np.uint64)
+    st = np.zeros(max(nt - 1, 1), dtype=np.uint64)
+    fs = C.create_string_buffer(n * T) if final_states else None
+    res = _PtResult()
+    res.state = C.cast(state, C.c_char_p)
+    res.chain_energies = _dptr(ce)
+    res.final_temps = ft.ctypes.data_as(C.POINTER(C.c_int32))
+    res.final_energies = _dptr(fe)
+    res.final_states = C.cast(fs, C.c_char_p) if fs is not None else None
+    res.swaps_accepted = sa.ctypes.data_as(C.POINTER(C.c_uint64))
+    res.swaps_attempted = st.ctypes.data_as(C.POINTER(C.c_uint64))
+    _check(lib().os_pt_run_sparse(ctx.handle, C.byref(q), C.byref(prm), C.byref(res)))
+    return TemperResult(np.frombuffer(state.raw[:n], dtype=np.uint8).copy(), res.energy, ce,
+                        ft.reshape(num_chains, nt), fe.reshape(num_chains, nt),
+                        np.frombuffer(fs.raw[: n * T], dtype=np.uint8).reshape(num_chains, nt, n).copy()
+                        if fs is not None else None,
+                        sa[: nt - 1], st[: nt - 1], res.max_field_drift, int(res.attempts), int(res.accepted),
+                        res.device_ms)
+
+
+def pt_exchange_replay(beta: Sequence[float], energies: np.ndarray, temps: np.ndarray, *, seed: int = 1234,
+                       round0: int = 0, num_rounds: int = 1, ctx: Optional[Context] = None):
+    """The exchange step of temper_sparse alone, on the GPU, with fixed
+    energies (chains x temps); returns (temps after the rounds, accepted
+    exchanges per adjacent pair)."""
+    ctx = ctx or default_context()
+    b = np.ascontiguousarray(beta, dtype=np.float64)
+    e = np.ascontiguousarray(energies, dtype=np.float64)
+    t = np.ascontiguousarray(temps, dtype=np.int32).copy()
+    chains, nt = t.shape
+    sw = np.zeros(max(nt - 1, 1), dtype=np.uint64)
+    _check(lib().os_pt_exchange_replay(ctx.handle, chains, nt, _dptr(b), _dptr(e), seed, round0, num_rounds,
+                                       t.ctypes.data_as(C.POINTER(C.c_int32)),
+                                       sw.ctypes.data_as(C.POINTER(C.c_uint64))))
+    return t, sw[: nt - 1]
 
 
 def _batch_inputs(instances):

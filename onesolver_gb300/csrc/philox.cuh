@@ -58,7 +58,13 @@ enum : uint32_t {
   kStreamInit = 0x1u << 28,    // initial spins
   kStreamSweep = 0x2u << 28,   // acceptance uniforms (sequential sites)
   kStreamSite = 0x3u << 28,    // site index + uniform (random sites)
+  kStreamExchange = 0x4u << 28,  // replica-exchange uniforms (tempering)
 };
+
+// Uniform in (0, 1) in FP64 from one 32-bit word: (r + 0.5) * 2^-32, exact.
+__host__ __device__ __forceinline__ double u01_open64(uint32_t r) {
+  return ((double)r + 0.5) * 0x1.0p-32;
+}
 
 }  // namespace os
 

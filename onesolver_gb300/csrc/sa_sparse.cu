@@ -50,6 +50,7 @@ struct SparseArgs {
   double *e;              // [T]
   double *ebest;          // [T]
   unsigned long long *accepted;
+  const int *temp;        // tempering: temperature index of each trajectory into beta
 };
 
 // Neighbour updates of a warp's accepted sites, applied once the colour is
@@ -76,6 +77,10 @@ __device__ __forceinline__ void apply_updates(const uint32_t *__restrict__ list,
   }
 }
 
+// TEMPER = false: annealing, beta[step / spb] from the schedule. TEMPER =
+// true: parallel tempering, each trajectory at its own fixed inverse
+// temperature beta[temp[t]] for the whole launch.
+template <bool TEMPER>
 __global__ void __launch_bounds__(256, 8) sa_sparse_kernel(const __grid_constant__ SparseArgs a) {
   extern __shared__ unsigned char smem[];
   const int R = a.traj_per_cta;
@@ -111,8 +116,10 @@ __global__ void __launch_bounds__(256, 8) sa_sparse_kernel(const __grid_constant
   const bool coop = a.deg_max <= 32;
   const int per = coop ? 32 / a.deg_max : 0;
   const int lr = coop ? lane / a.deg_max : 0, le = coop ? lane - lr * a.deg_max : 0;
+  float b_fixed = 1.f;
+  if constexpr (TEMPER) b_fixed = active ? (float)a.beta[a.temp[t]] : 1.f;
   for (int step = a.step_begin; step < a.step_end; ++step) {
-    const float b = (float)a.beta[step / a.spb];
+    const float b = TEMPER ? b_fixed : (float)a.beta[step / a.spb];
     float de = 0.f;
     for (int c = 0; c < a.ncolors; ++c) {
       const int c0 = a.color_ptr[c], cnt = a.color_ptr[c + 1] - c0;
@@ -451,13 +458,16 @@ void plan_create_sparse(os_sa_plan *p, const os_qubo_csr *q) {
   OS_REQUIRE(per <= 200 * 1024, "sparse instance too large for shared memory (%d variables)", n);
   p->traj_per_cta = R;
   p->warps = tpt * R / 32;
-  OS_CUDA(cudaFuncSetAttribute(sa_sparse_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               (int)std::max<size_t>(per * R, 48 * 1024)));
+  for (auto fn : {sa_sparse_kernel<false>, sa_sparse_kernel<true>})
+    OS_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)std::max<size_t>(per * R, 48 * 1024)));
 }
 
-void execute_sparse(os_sa_plan *p) {
+// Resets the counters, draws the initial spins and computes their FP64
+// fields and energies; returns the resync arguments (init = 0) for later
+// resyncs.
+static SparseResyncArgs start_sparse(os_sa_plan *p) {
   cudaStream_t s = p->ctx->stream;
-  p->launches = 0;
   const int n = p->n, T = p->T;
   OS_CUDA(cudaMemsetAsync(p->accepted.get(), 0, sizeof(unsigned long long) * T, s));
   OS_CUDA(cudaMemsetAsync(p->drift.get(), 0, sizeof(unsigned long long), s));
@@ -486,7 +496,10 @@ void execute_sparse(os_sa_plan *p) {
   OS_CUDA(cudaGetLastError());
   p->launches += 2;
   r.init = 0;
+  return r;
+}
 
+static SparseArgs sweep_args(os_sa_plan *p, const SparseResyncArgs &r) {
   SparseArgs a{};
   a.row_ptr = p->row_ptr.get();
   a.col = p->col.get();
@@ -495,13 +508,13 @@ void execute_sparse(os_sa_plan *p) {
   a.color_sites = p->color_sites.get();
   a.color_ptr = p->color_ptr.get();
   a.ncolors = p->ncolors;
-  a.n = n;
+  a.n = p->n;
   a.deg_max = p->deg_max;
   a.ell = p->ell.get();
   a.beta = p->beta.get();
   a.spb = p->spb;
   a.acceptance = p->acceptance;
-  a.T = T;
+  a.T = p->T;
   a.traj_per_cta = p->traj_per_cta;
   a.seed_lo = r.seed_lo;
   a.seed_hi = r.seed_hi;
@@ -512,6 +525,28 @@ void execute_sparse(os_sa_plan *p) {
   a.e = p->se.get();
   a.ebest = p->sebest.get();
   a.accepted = p->accepted.get();
+  a.temp = nullptr;
+  return a;
+}
+
+// FP64 re-score of the best state of every trajectory into p->e64.
+static void finish_sparse(os_sa_plan *p) {
+  cudaStream_t s = p->ctx->stream;
+  const int n = p->n, T = p->T;
+  OS_CUDA(cudaMemcpyAsync(p->states.get(), p->sxbest.get(), (size_t)T * n, cudaMemcpyDeviceToDevice, s));
+  sa_sparse_rescore_kernel<<<(T + 127) / 128, 128, 0, s>>>(p->row_ptr.get(), p->col.get(), p->val64.get(),
+                                                           p->diag64.get(), n, T, p->states.get(),
+                                                           p->e64.get());
+  OS_CUDA(cudaGetLastError());
+  p->launches += 1;
+}
+
+void execute_sparse(os_sa_plan *p) {
+  cudaStream_t s = p->ctx->stream;
+  p->launches = 0;
+  const int n = p->n, T = p->T;
+  const SparseResyncArgs r = start_sparse(p);
+  SparseArgs a = sweep_args(p, r);
   const int R = p->traj_per_cta;
   const int threads = p->warps * 32;
   const size_t smem = (size_t)n * 5 * R;
@@ -521,7 +556,7 @@ void execute_sparse(os_sa_plan *p) {
     a.step_begin = s0;
     a.step_end = std::min(p->steps, s0 + p->chunk);
     OS_CUDA(cudaEventRecord(p->event(2 * p->sweep_ev_used), s));
-    sa_sparse_kernel<<<grid, threads, smem, s>>>(a);
+    sa_sparse_kernel<false><<<grid, threads, smem, s>>>(a);
     OS_CUDA(cudaGetLastError());
     OS_CUDA(cudaEventRecord(p->event(2 * p->sweep_ev_used + 1), s));
     ++p->sweep_ev_used;
@@ -529,12 +564,218 @@ void execute_sparse(os_sa_plan *p) {
     OS_CUDA(cudaGetLastError());
     p->launches += 2;
   }
-  OS_CUDA(cudaMemcpyAsync(p->states.get(), p->sxbest.get(), (size_t)T * n, cudaMemcpyDeviceToDevice, s));
-  sa_sparse_rescore_kernel<<<(T + 127) / 128, 128, 0, s>>>(p->row_ptr.get(), p->col.get(), p->val64.get(),
-                                                           p->diag64.get(), n, T, p->states.get(),
-                                                           p->e64.get());
+  finish_sparse(p);
+}
+
+// ---------------------------------------------------------------------------
+// Parallel tempering (replica exchange; Swendsen and Wang, PRL 57 (1986);
+// Hukushima and Nemoto, J. Phys. Soc. Jpn. 65 (1996)). No counterpart in the
+// reference, whose annealing benchmark names it as the next solver
+// (benchmarks/annealing/performance.md:52-59). Replicas keep their spins and
+// fields; exchanges swap temperature labels only, so a round costs the sweep
+// launch plus one thread per chain.
+// ---------------------------------------------------------------------------
+
+struct ExchangeArgs {
+  const double *beta;          // [nt] inverse temperatures
+  const double *e;             // [chains * nt] current energies
+  int *temp;                   // [chains * nt] temperature index of each replica
+  int *traj_at;                // [chains][nt] replica at each temperature
+  unsigned long long *swaps;   // [nt - 1] accepted exchanges per pair
+  int chains, nt, round0, rounds;
+  uint32_t seed_lo, seed_hi;
+};
+
+// Rounds round0 .. round0 + rounds - 1 of the exchange step, one thread per
+// chain: pairs (k, k+1) with k = round mod 2, k + 2, ...; the pair swaps when
+// ln u < (beta[k+1] - beta[k]) * (E_cold - E_hot), i.e. with probability
+// min(1, exp(...)), u from Philox (pair, round, chain) and drawn only when
+// the exponent is negative.
+__global__ void pt_exchange_kernel(const __grid_constant__ ExchangeArgs a) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= a.chains) return;
+  int *at = a.traj_at + (size_t)c * a.nt;
+  for (int r = a.round0; r < a.round0 + a.rounds; ++r) {
+    for (int k = r & 1; k + 1 < a.nt; k += 2) {
+      const int hot = at[k], cold = at[k + 1];
+      const double d = (a.beta[k + 1] - a.beta[k]) * (a.e[cold] - a.e[hot]);
+      bool swap = d >= 0.0;
+      if (!swap) {
+        const Philox4 p = philox4x32_10((uint32_t)k, (uint32_t)r, (uint32_t)c, kStreamExchange, a.seed_lo,
+                                        a.seed_hi);
+        swap = log(u01_open64(p.x)) < d;
+      }
+      if (swap) {
+        at[k] = cold;
+        at[k + 1] = hot;
+        a.temp[cold] = k;
+        a.temp[hot] = k + 1;
+        atomicAdd(&a.swaps[k], 1ull);
+      }
+    }
+  }
+}
+
+// Replica t = chain * nt + r starts at temperature r.
+__global__ void pt_identity_kernel(int *temp, int *traj_at, int total, int nt) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= total) return;
+  temp[t] = t % nt;
+  traj_at[t] = t;
+}
+
+static void check_ladder(const double *beta, int nt) {
+  OS_REQUIRE(beta != nullptr && nt >= 1, "empty temperature ladder");
+  for (int k = 0; k < nt; ++k) {
+    OS_REQUIRE(std::isfinite(beta[k]) && beta[k] >= 0.0, "beta[%d] must be finite and >= 0", k);
+    OS_REQUIRE(k == 0 || beta[k] >= beta[k - 1], "beta must be non-decreasing (beta[%d] < beta[%d])", k, k - 1);
+  }
+}
+
+struct PtRun {
+  os_sa_plan p;                // sparse buffers; T = chains * nt, beta = the ladder
+  int chains = 0, nt = 0, rounds = 0, spr = 0, resync = 0;
+  os::DevBuf<int> temp, traj_at;
+  os::DevBuf<unsigned long long> swaps;
+  os::DevBuf<double> efinal;   // FP64 energies of the final states
+  cudaEvent_t ev[2] = {nullptr, nullptr};
+  ~PtRun() {
+    for (auto e : ev)
+      if (e) cudaEventDestroy(e);
+  }
+};
+
+static void pt_create(PtRun &pr, os_ctx *ctx, const os_qubo_csr *q, const os_pt_params *prm) {
+  OS_REQUIRE(prm != nullptr && q != nullptr, "null argument");
+  check_ladder(prm->beta, prm->num_temps);
+  OS_REQUIRE(prm->num_chains >= 1, "num_chains must be positive");
+  OS_REQUIRE(prm->num_rounds >= 1 && prm->sweeps_per_round >= 1, "num_rounds and sweeps_per_round must be positive");
+  OS_REQUIRE(prm->resync_every >= 0, "resync_every must be >= 0");
+  const unsigned long long total = (unsigned long long)prm->num_chains * (unsigned long long)prm->num_temps;
+  OS_REQUIRE(total <= 65535, "parallel tempering runs at most 65535 replicas (chains x temperatures)");
+  const long long steps = (long long)prm->num_rounds * prm->sweeps_per_round;
+  OS_REQUIRE(steps < (1ll << 31), "too many sweeps (%lld)", steps);
+  os_sa_params sp{};
+  sp.beta = prm->beta;
+  sp.num_iter = prm->num_temps;
+  sp.sweeps_per_beta = 1;
+  sp.num_tries = (uint32_t)total;
+  sp.seed = prm->seed;
+  sp.acceptance = OS_ACCEPT_PHYSICAL;
+  sp.site_order = OS_SITES_SEQUENTIAL;
+  sp.resync_every = 0;
+  sp.init_prob = nullptr;
+  pr.p.kind = 1;
+  os_sa_plan_common(&pr.p, ctx, &sp, q->n);
+  plan_create_sparse(&pr.p, q);
+  pr.p.steps = (int)steps;
+  pr.chains = (int)prm->num_chains;
+  pr.nt = prm->num_temps;
+  pr.rounds = prm->num_rounds;
+  pr.spr = prm->sweeps_per_round;
+  pr.resync = prm->resync_every;
+  pr.temp.alloc(total);
+  pr.traj_at.alloc(total);
+  pr.swaps.alloc(std::max(pr.nt - 1, 1));
+  pr.efinal.alloc(total);
+  for (auto &e : pr.ev) OS_CUDA(cudaEventCreate(&e));
+}
+
+static void pt_execute(PtRun &pr) {
+  os_sa_plan *p = &pr.p;
+  cudaStream_t s = p->ctx->stream;
+  p->launches = 0;
+  const int n = p->n, T = p->T;
+  OS_CUDA(cudaMemsetAsync(pr.swaps.get(), 0, sizeof(unsigned long long) * pr.swaps.count, s));
+  pt_identity_kernel<<<(T + 127) / 128, 128, 0, s>>>(pr.temp.get(), pr.traj_at.get(), T, pr.nt);
   OS_CUDA(cudaGetLastError());
-  p->launches += 1;
+  const SparseResyncArgs r = start_sparse(p);
+  SparseArgs a = sweep_args(p, r);
+  a.temp = pr.temp.get();
+  ExchangeArgs x{};
+  x.beta = p->beta.get();
+  x.e = p->se.get();
+  x.temp = pr.temp.get();
+  x.traj_at = pr.traj_at.get();
+  x.swaps = pr.swaps.get();
+  x.chains = pr.chains;
+  x.nt = pr.nt;
+  x.rounds = 1;
+  x.seed_lo = r.seed_lo;
+  x.seed_hi = r.seed_hi;
+  const int R = p->traj_per_cta;
+  const int threads = p->warps * 32;
+  const size_t smem = (size_t)n * 5 * R;
+  const int grid = (T + R - 1) / R;
+  OS_CUDA(cudaEventRecord(pr.ev[0], s));
+  for (int round = 0; round < pr.rounds; ++round) {
+    a.step_begin = round * pr.spr;
+    a.step_end = a.step_begin + pr.spr;
+    sa_sparse_kernel<true><<<grid, threads, smem, s>>>(a);
+    OS_CUDA(cudaGetLastError());
+    ++p->launches;
+    if (pr.nt > 1) {
+      x.round0 = round;
+      pt_exchange_kernel<<<(pr.chains + 127) / 128, 128, 0, s>>>(x);
+      OS_CUDA(cudaGetLastError());
+      ++p->launches;
+    }
+    // Same resync points as an anneal whose chunk is resync_every rounds.
+    if ((pr.resync > 0 && (round + 1) % pr.resync == 0) || round + 1 == pr.rounds) {
+      sa_sparse_resync_kernel<<<T, 256, 0, s>>>(r);
+      OS_CUDA(cudaGetLastError());
+      ++p->launches;
+    }
+  }
+  OS_CUDA(cudaEventRecord(pr.ev[1], s));
+  finish_sparse(p);
+  sa_sparse_rescore_kernel<<<(T + 127) / 128, 128, 0, s>>>(p->row_ptr.get(), p->col.get(), p->val64.get(),
+                                                           p->diag64.get(), n, T, p->sx.get(), pr.efinal.get());
+  OS_CUDA(cudaGetLastError());
+  ++p->launches;
+}
+
+static void pt_result(PtRun &pr, os_pt_result *res) {
+  OS_REQUIRE(res != nullptr, "null result");
+  os_sa_plan *p = &pr.p;
+  OS_CUDA(cudaStreamSynchronize(p->ctx->stream));
+  const int T = p->T, n = p->n;
+  std::vector<double> e(T);
+  OS_CUDA(cudaMemcpy(e.data(), p->e64.get(), sizeof(double) * T, cudaMemcpyDeviceToHost));
+  std::vector<unsigned long long> acc(T);
+  OS_CUDA(cudaMemcpy(acc.data(), p->accepted.get(), sizeof(unsigned long long) * T, cudaMemcpyDeviceToHost));
+  unsigned long long drift_bits = 0;
+  OS_CUDA(cudaMemcpy(&drift_bits, p->drift.get(), sizeof drift_bits, cudaMemcpyDeviceToHost));
+  const int best = argmin_first(e);
+  if (res->state) OS_CUDA(cudaMemcpy(res->state, p->states.get() + (size_t)best * n, n, cudaMemcpyDeviceToHost));
+  res->energy = e[best];
+  if (res->chain_energies)
+    for (int c = 0; c < pr.chains; ++c) {
+      double m = e[(size_t)c * pr.nt];
+      for (int k = 1; k < pr.nt; ++k) m = std::min(m, e[(size_t)c * pr.nt + k]);
+      res->chain_energies[c] = m;
+    }
+  if (res->final_temps)
+    OS_CUDA(cudaMemcpy(res->final_temps, pr.temp.get(), sizeof(int) * T, cudaMemcpyDeviceToHost));
+  if (res->final_energies)
+    OS_CUDA(cudaMemcpy(res->final_energies, pr.efinal.get(), sizeof(double) * T, cudaMemcpyDeviceToHost));
+  if (res->final_states) OS_CUDA(cudaMemcpy(res->final_states, p->sx.get(), (size_t)T * n, cudaMemcpyDeviceToHost));
+  if (pr.nt > 1 && res->swaps_accepted)
+    OS_CUDA(cudaMemcpy(res->swaps_accepted, pr.swaps.get(), sizeof(unsigned long long) * (pr.nt - 1),
+                       cudaMemcpyDeviceToHost));
+  if (res->swaps_attempted)
+    for (int k = 0; k + 1 < pr.nt; ++k)  // rounds with round mod 2 == k mod 2
+      res->swaps_attempted[k] = (unsigned long long)pr.chains * (unsigned long long)((pr.rounds + 1 - (k & 1)) / 2);
+  double drift;
+  std::memcpy(&drift, &drift_bits, sizeof drift);
+  res->max_field_drift = drift;
+  res->attempts = (unsigned long long)p->steps * (unsigned long long)n * (unsigned long long)T;
+  unsigned long long total = 0;
+  for (auto v : acc) total += v;
+  res->accepted = total;
+  float ms = 0.f;
+  OS_CUDA(cudaEventElapsedTime(&ms, pr.ev[0], pr.ev[1]));
+  res->device_ms = ms;
 }
 
 }  // namespace sa
@@ -577,6 +818,76 @@ os_status os_sa_run_sparse(os_ctx *ctx, const os_qubo_csr *qubo, const os_sa_par
   if (st == OS_OK) st = os_sa_plan_result(plan, result);
   os_sa_plan_destroy(plan);
   return st;
+}
+
+
+os_status os_pt_run_sparse(os_ctx *ctx, const os_qubo_csr *qubo, const os_pt_params *params,
+                           os_pt_result *result) {
+  return guard([&] {
+    activate(ctx);
+    OS_REQUIRE(result != nullptr, "null result");
+    PtRun pr;
+    pt_create(pr, ctx, qubo, params);
+    pt_execute(pr);
+    pt_result(pr, result);
+  });
+}
+
+os_status os_pt_exchange_replay(os_ctx *ctx, uint32_t num_chains, int32_t num_temps, const double *beta,
+                                const double *energies, uint64_t seed, int32_t round0, int32_t num_rounds,
+                                int32_t *temps, uint64_t *swaps_accepted) {
+  return guard([&] {
+    activate(ctx);
+    check_ladder(beta, num_temps);
+    OS_REQUIRE(num_chains >= 1, "num_chains must be positive");
+    OS_REQUIRE(round0 >= 0 && num_rounds >= 0, "rounds must be >= 0");
+    OS_REQUIRE(energies != nullptr && temps != nullptr, "null argument");
+    const size_t total = (size_t)num_chains * (size_t)num_temps;
+    OS_REQUIRE(total <= (1u << 30), "too many replicas");
+    std::vector<int> at(total, -1);
+    for (size_t c = 0; c < num_chains; ++c)
+      for (int r = 0; r < num_temps; ++r) {
+        const int k = temps[c * num_temps + r];
+        OS_REQUIRE(k >= 0 && k < num_temps && at[c * num_temps + k] < 0,
+                   "temps of chain %zu is not a permutation", c);
+        at[c * num_temps + k] = (int)(c * num_temps + r);
+      }
+    cudaStream_t s = ctx->stream;
+    DevBuf<double> b, e;
+    DevBuf<int> t, ta;
+    DevBuf<unsigned long long> sw;
+    b.alloc(num_temps);
+    e.alloc(total);
+    t.alloc(total);
+    ta.alloc(total);
+    sw.alloc(std::max(num_temps - 1, 1));
+    OS_CUDA(cudaMemcpyAsync(b.get(), beta, sizeof(double) * num_temps, cudaMemcpyHostToDevice, s));
+    OS_CUDA(cudaMemcpyAsync(e.get(), energies, sizeof(double) * total, cudaMemcpyHostToDevice, s));
+    OS_CUDA(cudaMemcpyAsync(t.get(), temps, sizeof(int) * total, cudaMemcpyHostToDevice, s));
+    OS_CUDA(cudaMemcpyAsync(ta.get(), at.data(), sizeof(int) * total, cudaMemcpyHostToDevice, s));
+    OS_CUDA(cudaMemsetAsync(sw.get(), 0, sizeof(unsigned long long) * sw.count, s));
+    ExchangeArgs x{};
+    x.beta = b.get();
+    x.e = e.get();
+    x.temp = t.get();
+    x.traj_at = ta.get();
+    x.swaps = sw.get();
+    x.chains = (int)num_chains;
+    x.nt = num_temps;
+    x.round0 = round0;
+    x.rounds = num_rounds;
+    x.seed_lo = (uint32_t)seed;
+    x.seed_hi = (uint32_t)(seed >> 32);
+    if (num_rounds > 0) {
+      pt_exchange_kernel<<<(unsigned)ceil_div_u64(num_chains, 128), 128, 0, s>>>(x);
+      OS_CUDA(cudaGetLastError());
+    }
+    OS_CUDA(cudaMemcpyAsync(temps, t.get(), sizeof(int) * total, cudaMemcpyDeviceToHost, s));
+    if (swaps_accepted && num_temps > 1)
+      OS_CUDA(cudaMemcpyAsync(swaps_accepted, sw.get(), sizeof(unsigned long long) * (num_temps - 1),
+                              cudaMemcpyDeviceToHost, s));
+    OS_CUDA(cudaStreamSynchronize(s));
+  });
 }
 
 }  // extern "C"

@@ -68,6 +68,8 @@ def lib() -> C.CDLL:
         L.orc_argmin.restype = C.c_int
         L.orc_philox4x32_10.argtypes = [C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]
         L.orc_philox4x32_10.restype = None
+        L.orc_pt_exchange.argtypes = [C.c_int, C.c_int, _D, _D, C.c_uint64, C.c_int, C.c_int, _I, _U64]
+        L.orc_pt_exchange.restype = None
         L.orc_solution_csv.argtypes = [C.c_char_p, C.c_int, C.c_double, C.c_char_p, C.c_int]
         L.orc_solution_csv.restype = C.c_int
         _lib = L
@@ -185,6 +187,19 @@ def philox(ctr, key) -> list[int]:
     o = (C.c_uint32 * 4)()
     lib().orc_philox4x32_10(c, k, o)
     return list(o)
+
+
+def pt_exchange(beta, energies, seed: int, round0: int, rounds: int, temps):
+    """Replica-exchange rounds with fixed energies (energies, temps: chains x nt);
+    returns (temps after the rounds, accepted exchanges per adjacent pair)."""
+    b = np.ascontiguousarray(beta, dtype=np.float64)
+    e = np.ascontiguousarray(energies, dtype=np.float64)
+    t = np.ascontiguousarray(temps, dtype=np.int32).copy()
+    chains, nt = t.shape
+    sw = np.zeros(max(nt - 1, 1), dtype=np.uint64)
+    lib().orc_pt_exchange(chains, nt, _d(b), _d(e), seed, round0, rounds,
+                          t.ctypes.data_as(_I), sw.ctypes.data_as(_U64))
+    return t, sw[: nt - 1]
 
 
 def solution_csv(state, energy_value: float) -> str:

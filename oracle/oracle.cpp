@@ -424,4 +424,47 @@ int orc_solution_csv(const char *state, int n, double energy, char *out, int cap
   return (int)s.size();
 }
 
+
+// Replica-exchange step of parallel tempering (Swendsen and Wang, PRL 57
+// (1986); Hukushima and Nemoto, J. Phys. Soc. Jpn. 65 (1996)). Not in the
+// reference: its annealing benchmark recommends parallel tempering as the
+// next solver (benchmarks/annealing/performance.md:52-59), so this is the
+// project's own statement of the rule the GPU library implements, written
+// independently of it. Chains of nt replicas; temps[c*nt + r] is the
+// temperature index of replica r of chain c. Round `round` tries the adjacent
+// pairs (k, k+1), k = round mod 2, k+2, ...; with `hot` the replica at k and
+// `cold` the one at k+1, d = (beta[k+1] - beta[k]) * (E_cold - E_hot), and the
+// pair swaps when d >= 0 or ln u < d, u = (w + 1/2) 2^-32 with w the first
+// word of Philox4x32-10 at counter (k, round, c, 4 << 28) and key (seed low,
+// seed high). Energies are held fixed; swaps[k] counts accepted exchanges.
+void orc_pt_exchange(int chains, int nt, const double *beta, const double *e, uint64_t seed, int round0,
+                     int rounds, int *temps, uint64_t *swaps) {
+  std::vector<int> at((size_t)chains * nt);
+  for (int c = 0; c < chains; ++c)
+    for (int r = 0; r < nt; ++r) at[(size_t)c * nt + temps[(size_t)c * nt + r]] = c * nt + r;
+  for (int k = 0; k + 1 < nt; ++k) swaps[k] = 0;
+  const uint32_t key[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)};
+  for (int c = 0; c < chains; ++c) {
+    int *a = &at[(size_t)c * nt];
+    for (int round = round0; round < round0 + rounds; ++round)
+      for (int k = round % 2; k + 1 < nt; k += 2) {
+        const int hot = a[k], cold = a[k + 1];
+        const double d = (beta[k + 1] - beta[k]) * (e[cold] - e[hot]);
+        bool swap = d >= 0.0;
+        if (!swap) {
+          const uint32_t ctr[4] = {(uint32_t)k, (uint32_t)round, (uint32_t)c, 4u << 28};
+          uint32_t w[4];
+          philox4x32_10(ctr, key, w);
+          swap = std::log(((double)w[0] + 0.5) * 0x1.0p-32) < d;
+        }
+        if (swap) {
+          std::swap(a[k], a[k + 1]);
+          temps[cold] = k;
+          temps[hot] = k + 1;
+          ++swaps[k];
+        }
+      }
+  }
+}
+
 }  // extern "C"
