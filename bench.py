@@ -24,7 +24,7 @@ Workloads (--workload):
                 of a long plain-SA best) of the gated warm start vs plain
                 random-init SA, 512 trajectories each. Metric: seconds.
   pt-droplet    Parallel tempering on the reference's Chimera droplet 512/001
-                (committed fixture): 32 chains x 32 temperatures, 2,000
+                (committed fixture): 128 chains x 32 temperatures, 2,000
                 exchange rounds of 5 sweeps. Metric: spin-flip attempts/s;
                 the best energies are reported against the tensor-network
                 ground state and the reference's best published SA energy.
@@ -460,7 +460,7 @@ def bench_pt(args, ctx, pg, rank, world):
     csr = osg.Csr.from_dense(f)
     n = csr.n
     beta = np.geomspace(0.05, 3.0, 32)
-    chains, rounds, spr, resync = 32, 2000, 5, 200
+    chains, rounds, spr, resync = 128, 2000, 5, 200
     T = chains * len(beta)
     attempts = T * rounds * spr * n
     run = lambda: osg.temper_sparse(csr, beta, num_chains=chains, num_rounds=rounds, sweeps_per_round=spr,
@@ -690,12 +690,12 @@ CONFIG_NAMES = {
     "sa-batch": "batched dense SA, 512 instances n~U[64,1024], 256 trajectories x 2,000 sweeps",
     "sa-n64": "dense SA, n=64, 100 trajectories x 100 steps (reference CLI defaults)",
     "sa-learned": "SK n=1024 learned warm start, time-to-target",
-    "pt-droplet": "parallel tempering, Chimera droplet 512/001, 32 chains x 32 temperatures x 10,000 sweeps",
+    "pt-droplet": "parallel tempering, Chimera droplet 512/001, 128 chains x 32 temperatures x 10,000 sweeps",
 }
 
 
 PROFILE_CASES = ("exhaustive32", "exhaustive36", "sa-sk1024", "sa-batch48", "sa-batch128x256", "sa-chimera",
-                 "mpnn-predict1024")
+                 "mpnn-predict1024", "pt-droplet512")
 
 
 def profile_case(name: str, ctx) -> None:
@@ -724,6 +724,14 @@ def profile_case(name: str, ctx) -> None:
     elif name == "sa-chimera":
         plan = osg.AnnealPlan(chimera_csr(16, 0), osg.linear_schedule(0.1, 2.9, 50), num_tries=1024,
                               acceptance=osg.ACCEPT_PHYSICAL, ctx=ctx)
+    elif name == "pt-droplet512":
+        g = json.loads((ROOT / "tests" / "golden" / "chimera_golden.json").read_text())["512"]
+        csr = osg.Csr.from_dense(osg.Model.load(ROOT / "tests" / "golden" / g["file"]).flatten())
+        r = osg.temper_sparse(csr, np.geomspace(0.05, 3.0, 32), num_chains=128, num_rounds=20, sweeps_per_round=5,
+                              resync_every=200, ctx=ctx)
+        torch.cuda.synchronize()
+        print(json.dumps({"profile_case": name, "energy": r.energy, "device_ms": r.device_ms}))
+        return
     elif name == "mpnn-predict1024":
         net = osg.WarmStartNet(seed=1, ctx=ctx)
         p = net.predict(sk_qubo(1024, 3))

@@ -10,7 +10,10 @@ a thin ctypes mirror of that ABI and of the reference's user-facing calls:
 * :func:`anneal` / :func:`anneal_sparse` -- ``sa::anneal``
   (``include/simulated_annealing/annealing.hpp``);
 * :func:`linear_schedule` / :func:`geometric_schedule` -- the CLI's beta
-  schedules (``app/one-solver-anneal.cpp:23-39``).
+  schedules (``app/one-solver-anneal.cpp:23-39``);
+* :func:`temper_sparse` -- parallel tempering on the sparse sweep kernel (no
+  reference counterpart; ``benchmarks/annealing/performance.md:52-59`` names
+  it as the next solver).
 
 There is no CPU fallback: every solver call runs on the GPU through the native
 library, and importing the library fails loudly when it has not been built.

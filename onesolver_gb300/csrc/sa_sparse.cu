@@ -586,17 +586,20 @@ struct ExchangeArgs {
   uint32_t seed_lo, seed_hi;
 };
 
-// Rounds round0 .. round0 + rounds - 1 of the exchange step, one thread per
-// chain: pairs (k, k+1) with k = round mod 2, k + 2, ...; the pair swaps when
+// Rounds round0 .. round0 + rounds - 1 of the exchange step, one warp per
+// chain: the pairs (k, k+1) of a round, k = round mod 2, k + 2, ..., are
+// disjoint, so lane l takes the pairs k = round mod 2 + 2 (l + 32 i) and the
+// round needs one pass of loads; the pair swaps when
 // ln u < (beta[k+1] - beta[k]) * (E_cold - E_hot), i.e. with probability
 // min(1, exp(...)), u from Philox (pair, round, chain) and drawn only when
 // the exponent is negative.
 __global__ void pt_exchange_kernel(const __grid_constant__ ExchangeArgs a) {
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  const long long c = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;  // warp-uniform
   if (c >= a.chains) return;
-  int *at = a.traj_at + (size_t)c * a.nt;
+  int *at = a.traj_at + c * a.nt;
   for (int r = a.round0; r < a.round0 + a.rounds; ++r) {
-    for (int k = r & 1; k + 1 < a.nt; k += 2) {
+    for (int k = (r & 1) + 2 * lane; k + 1 < a.nt; k += 64) {
       const int hot = at[k], cold = at[k + 1];
       const double d = (a.beta[k + 1] - a.beta[k]) * (a.e[cold] - a.e[hot]);
       bool swap = d >= 0.0;
@@ -613,8 +616,12 @@ __global__ void pt_exchange_kernel(const __grid_constant__ ExchangeArgs a) {
         atomicAdd(&a.swaps[k], 1ull);
       }
     }
+    __syncwarp();  // the next round reads pairs that other lanes wrote
   }
 }
+
+// Grid of the exchange kernel: 4 chains (warps) per 128-thread block.
+static unsigned exchange_blocks(unsigned long long chains) { return (unsigned)ceil_div_u64(chains, 4); }
 
 // Replica t = chain * nt + r starts at temperature r.
 __global__ void pt_identity_kernel(int *temp, int *traj_at, int total, int nt) {
@@ -716,7 +723,7 @@ static void pt_execute(PtRun &pr) {
     ++p->launches;
     if (pr.nt > 1) {
       x.round0 = round;
-      pt_exchange_kernel<<<(pr.chains + 127) / 128, 128, 0, s>>>(x);
+      pt_exchange_kernel<<<exchange_blocks(pr.chains), 128, 0, s>>>(x);
       OS_CUDA(cudaGetLastError());
       ++p->launches;
     }
@@ -879,7 +886,7 @@ os_status os_pt_exchange_replay(os_ctx *ctx, uint32_t num_chains, int32_t num_te
     x.seed_lo = (uint32_t)seed;
     x.seed_hi = (uint32_t)(seed >> 32);
     if (num_rounds > 0) {
-      pt_exchange_kernel<<<(unsigned)ceil_div_u64(num_chains, 128), 128, 0, s>>>(x);
+      pt_exchange_kernel<<<exchange_blocks(num_chains), 128, 0, s>>>(x);
       OS_CUDA(cudaGetLastError());
     }
     OS_CUDA(cudaMemcpyAsync(temps, t.get(), sizeof(int) * total, cudaMemcpyDeviceToHost, s));

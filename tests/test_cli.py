@@ -145,3 +145,45 @@ def test_anneal_cli_on_the_chimera_fixture(apps, tmp_path):
     # (six significant digits, solution.hpp:58-67).
     e = oracle.energy(f, np.array(bits, dtype=np.uint8))
     assert out.read_text().splitlines()[1].split(",")[-1] == f"{e:g}"
+
+
+# ---------------------------------------------------------------------------
+# one-solver-temper (parallel tempering; no reference counterpart)
+# ---------------------------------------------------------------------------
+
+@pytest.fixture(scope="module")
+def temper():
+    return {p.name: p for p in nbuild.build_apps()}["one-solver-temper"]
+
+
+def test_temper_help_and_checks(temper, small_input, tmp_path):
+    rc, out, _ = run(temper, "--help")
+    assert rc == 0
+    for opt in ("--input", "--output", "--num-temps", "--num-chains", "--num-rounds", "--sweeps-per-round",
+                "--beta-min", "--beta-max", "--device-type", "--seed", "--resync-every"):
+        assert opt in out
+    rc, _, err = run(temper)
+    assert rc == 255 and "No input file provided." in err
+    _, path = small_input
+    for args, msg in [(("--beta-min", "2", "--beta-max", "1"), "beta-min is greater than beta-max"),
+                      (("--beta-min", "0"), "both ends of beta range need to be positive"),
+                      (("--num-temps", "0"), "num-temps must be positive"),
+                      (("--device-type", "fpga"), "Unknown device type: fpga")]:
+        rc, _, err = run(temper, "--input", path, "--output", tmp_path / "o.csv", *args)
+        assert rc == 255 and msg in err, (args, err)
+    rc, _, err = run(temper, "--input", path, "--output", tmp_path / "o.csv", "--device-type", "host")
+    assert rc == 1 and "No devices of given type could be initialized." in err
+
+
+@pytest.mark.gpu
+def test_temper_cli_reaches_the_droplet_ground_state(temper, tmp_path, golden_chimera):
+    src = ROOT / "tests" / "golden" / "chimera_128_001.qubo"
+    f = dense_from_text(src.read_text())
+    out = tmp_path / "o.csv"
+    rc, stdout, err = run(temper, "--input", src, "--output", out, "--num-chains", "64", "--num-rounds", "800")
+    assert rc == 0, err
+    assert "Using device:" in stdout
+    bits, energy, _ = read_csv(out)
+    e = oracle.energy(f, np.array(bits, dtype=np.uint8))
+    assert abs(e - golden_chimera["128"]["tn_ground_qubo"]) < 1e-6
+    assert out.read_text().splitlines()[1].split(",")[-1] == f"{e:g}"
