@@ -24,7 +24,7 @@ Workloads (--workload):
                 of a long plain-SA best) of the gated warm start vs plain
                 random-init SA, 512 trajectories each. Metric: seconds.
   pt-droplet    Parallel tempering on the reference's Chimera droplet 512/001
-                (committed fixture): 128 chains x 32 temperatures, 2,000
+                (committed fixture): 128 chains x 32 temperatures, 20,000
                 exchange rounds of 5 sweeps. Metric: spin-flip attempts/s;
                 the best energies are reported against the tensor-network
                 ground state and the reference's best published SA energy.
@@ -460,12 +460,12 @@ def bench_pt(args, ctx, pg, rank, world):
     csr = osg.Csr.from_dense(f)
     n = csr.n
     beta = np.geomspace(0.05, 3.0, 32)
-    chains, rounds, spr, resync = 128, 2000, 5, 200
+    chains, rounds, spr, resync = 128, 20000, 5, 200
     T = chains * len(beta)
     attempts = T * rounds * spr * n
     run = lambda: osg.temper_sparse(csr, beta, num_chains=chains, num_rounds=rounds, sweeps_per_round=spr,
                                     resync_every=resync, seed=1000 * rank + len(dev_ms), ctx=ctx)
-    dev_ms, wall, best = [], [], []
+    dev_ms, wall, best, acc = [], [], [], []
     for _ in range(args.warmup):
         run()
     torch.cuda.synchronize()
@@ -478,11 +478,18 @@ def bench_pt(args, ctx, pg, rank, world):
         wall.append(time.perf_counter() - t0)
         dev_ms.append(r.device_ms)
         best.append(r.energy)
+        acc.append(r.accepted)
     clocks = sampler.stop()
     barrier(pg)
     t_dev = max_over_ranks(pg, statistics.mean(dev_ms))
     t_e2e = max_over_ranks(pg, statistics.mean(wall))
     launches = 3 + rounds * 2 + rounds // resync + 2
+    # Shared-memory bytes of the sweeps, as for the sparse anneal: 5 per
+    # attempt (field, spin) and 1 + 8 deg per accepted flip.
+    avg_deg = float(csr.row_ptr[-1]) / n
+    smem_bytes = 5.0 * attempts + statistics.mean(acc) * (1.0 + 8.0 * avg_deg)
+    achieved = smem_bytes / (t_dev * 1e-3) / 1e9
+    peak = osg.probe_smem_row_peak(ctx)
     h2d = csr.row_ptr.nbytes + csr.col.nbytes + csr.val.nbytes + csr.diag.nbytes + beta.nbytes
     return {
         "metric": "parallel-tempering spin-flip attempts/s", "value": world * attempts / (t_dev * 1e-3),
@@ -494,7 +501,12 @@ def bench_pt(args, ctx, pg, rank, world):
                    "timing": "device_ms: CUDA events around the rounds; e2e: the host-buffer call"},
         "result": {"best_energy_per_step": best, "tn_ground_qubo": g["tn_ground_qubo"],
                    "published_best_sa": g["published_best_sa"],
-                   "steps_at_tn_ground": sum(abs(b - g["tn_ground_qubo"]) < 1e-6 for b in best)},
+                   "steps_at_tn_ground": sum(abs(b - g["tn_ground_qubo"]) < 1e-6 for b in best),
+                   "acceptance_rate": statistics.mean(acc) / attempts},
+        "roofline": {"bound": "smem", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": None, "bytes_per_step": smem_bytes,
+                     "kernel_ms": t_dev, "note": "device time of the rounds (sweeps, exchanges, resyncs)",
+                     "peak_source": "os_probe_smem_row_peak measured in this run"},
         "e2e": {"value": world * attempts / t_e2e, "unit": "attempts/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(n + 8 * chains + 12 * T + 16 * (len(beta) - 1)), "ms_per_step": t_e2e * 1e3},
         "gpu_launches": launches * args.steps,
@@ -690,7 +702,7 @@ CONFIG_NAMES = {
     "sa-batch": "batched dense SA, 512 instances n~U[64,1024], 256 trajectories x 2,000 sweeps",
     "sa-n64": "dense SA, n=64, 100 trajectories x 100 steps (reference CLI defaults)",
     "sa-learned": "SK n=1024 learned warm start, time-to-target",
-    "pt-droplet": "parallel tempering, Chimera droplet 512/001, 128 chains x 32 temperatures x 10,000 sweeps",
+    "pt-droplet": "parallel tempering, Chimera droplet 512/001, 128 chains x 32 temperatures x 100,000 sweeps",
 }
 
 
@@ -782,7 +794,7 @@ def main():
         return
     if args.steps <= 0:
         args.steps = {"exhaustive36": 50, "sa-chimera": 10, "sa-sk": 5, "sa-batch": 3, "sa-n64": 50,
-                      "sa-learned": 1, "pt-droplet": 5}[args.workload]
+                      "sa-learned": 1, "pt-droplet": 3}[args.workload]
     args.warmup = max(args.warmup, 3)
 
     world, rank, local, pg = dist_setup(args.gpus)

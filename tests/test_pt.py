@@ -199,3 +199,17 @@ def test_tempering_rejects_bad_arguments(native, ctx):
         native.temper_sparse(csr, [1.0], num_rounds=0, ctx=ctx)
     with pytest.raises(native.OneSolverError, match="permutation"):
         native.pt_exchange_replay([0.1, 1.0], np.zeros((2, 2)), np.zeros((2, 2), np.int32), ctx=ctx)
+
+
+@pytest.mark.gpu
+def test_droplet_512_reaches_tensor_network_ground_state(native, orc, ctx, golden_chimera):
+    """Droplet 512/001: the reference's best SA energy is -674.96 and the
+    tensor-network ground state is -928.747; 10^5 sweeps of 128 chains x 32
+    temperatures (about 3 s on one GB300) reach it."""
+    from tests.conftest import GOLDEN
+    g = golden_chimera["512"]
+    f = native.Model.load(GOLDEN / g["file"]).flatten()
+    res = native.temper_sparse(native.Csr.from_dense(f), np.geomspace(0.05, 3.0, 32), num_chains=128,
+                               num_rounds=20000, sweeps_per_round=5, resync_every=200, seed=7, ctx=ctx)
+    assert res.energy == pytest.approx(orc.energy(f, res.state), rel=1e-9, abs=0)
+    assert abs(res.energy - g["tn_ground_qubo"]) < 1e-6, res.energy
