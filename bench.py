@@ -28,6 +28,10 @@ Workloads (--workload):
                 exchange rounds of 5 sweeps. Metric: spin-flip attempts/s;
                 the best energies are reported against the tensor-network
                 ground state and the reference's best published SA energy.
+  pa-droplet    Population annealing on the same fixture: 16,384 replicas,
+                1,000 steps of linear beta 0.05 -> 3.0 with 5 sweeps each.
+                Metric: spin-flip attempts/s; best energies and the final
+                free-energy estimate are reported.
   sa-n64        Dense SA, n = 64, N(0,1) entries (seed 0), 100 trajectories x
                 100 random-site steps, geometric beta 0.1 -> 1.0 with the
                 reference's acceptance rule. Metric: spin-flip attempts/s.
@@ -514,6 +518,58 @@ def bench_pt(args, ctx, pg, rank, world):
     }
 
 
+def bench_pa(args, ctx, pg, rank, world):
+    """Population annealing on the reference's Chimera droplet 512/001
+    (committed fixture): attempts/s, best energy, free-energy estimate."""
+    import torch
+    import onesolver_gb300 as osg
+    g = json.loads((ROOT / "tests" / "golden" / "chimera_golden.json").read_text())["512"]
+    f = osg.Model.load(ROOT / "tests" / "golden" / g["file"]).flatten()
+    csr = osg.Csr.from_dense(f)
+    n = csr.n
+    R, K, spb, resync = 16384, 1000, 5, 100
+    beta = np.linspace(0.05, 3.0, K)
+    attempts = R * K * spb * n
+    seeds = iter(range(10 ** 6))
+    run = lambda: osg.population_anneal_sparse(csr, beta, population=R, sweeps_per_beta=spb, resync_every=resync,
+                                               seed=1000 * rank + next(seeds), ctx=ctx)
+    for _ in range(args.warmup):
+        run()
+    torch.cuda.synchronize()
+    barrier(pg)
+    sampler = ClockSampler(torch.cuda.current_device())
+    sampler.start()
+    dev_ms, wall, best, fam, lz = [], [], [], [], []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        r = run()
+        wall.append(time.perf_counter() - t0)
+        dev_ms.append(r.device_ms)
+        best.append(r.energy)
+        fam.append(r.families)
+        lz.append(float(r.log_z[-1]))
+    clocks = sampler.stop()
+    barrier(pg)
+    t_dev = max_over_ranks(pg, statistics.mean(dev_ms))
+    t_e2e = max_over_ranks(pg, statistics.mean(wall))
+    h2d = csr.row_ptr.nbytes + csr.col.nbytes + csr.val.nbytes + csr.diag.nbytes + beta.nbytes
+    return {
+        "metric": "population-annealing spin-flip attempts/s", "value": world * attempts / (t_dev * 1e-3),
+        "unit": "attempts/s", "ms_per_step": t_dev, "dtype": "fp32",
+        "config": {"workload": f"population annealing, Chimera droplet 512/001 (reference fixture), {R} replicas, "
+                               f"{K} steps of linear beta 0.05->3.0 x {spb} sweeps, systematic resampling",
+                   "n": n, "population": R, "attempts_per_step": attempts,
+                   "timing": "device_ms: CUDA events around the steps; e2e: the host-buffer call"},
+        "result": {"best_energy_per_step": best, "families_per_step": fam, "log_z_final_per_step": lz,
+                   "tn_ground_qubo": g["tn_ground_qubo"], "published_best_sa": g["published_best_sa"],
+                   "steps_at_tn_ground": sum(abs(b - g["tn_ground_qubo"]) < 1e-6 for b in best)},
+        "e2e": {"value": world * attempts / t_e2e, "unit": "attempts/s", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(n + 8 * K + 8 * R + 12 * R), "ms_per_step": t_e2e * 1e3},
+        "gpu_launches": (3 + 3 * K + K // resync + 2) * args.steps,
+        "clocks": clocks,
+    }
+
+
 WARM_BETA_MIN = 2.0  # schedule of the warm-started runs and of their fair-coin control
 
 
@@ -662,9 +718,10 @@ def reference_arm(args, world, rank):
         return None
     threads = os.cpu_count() or 1
     w = args.workload
-    if w == "pt-droplet":
-        return {"impl": "reference", "unavailable": "the reference has no parallel tempering "
-                                                    "(benchmarks/annealing/performance.md names it as future work)"}
+    if w in ("pt-droplet", "pa-droplet"):
+        return {"impl": "reference", "unavailable": "the reference has no parallel tempering or population "
+                                                    "annealing (benchmarks/annealing/performance.md names them as "
+                                                    "future work)"}
     vals = []
     sample_desc = ""
     for i in range(args.warmup + args.steps):
@@ -694,6 +751,7 @@ METRICS = {
     "sa-n64": "SA spin-flip attempts/s",
     "sa-learned": "SA time-to-target, learned warm start vs plain",
     "pt-droplet": "parallel-tempering spin-flip attempts/s",
+    "pa-droplet": "population-annealing spin-flip attempts/s",
 }
 CONFIG_NAMES = {
     "exhaustive36": "exhaustive search, dense QUBO n=36, integer Q_ij ~ U{-8..8} (seed 0), 2^36 states",
@@ -703,6 +761,7 @@ CONFIG_NAMES = {
     "sa-n64": "dense SA, n=64, 100 trajectories x 100 steps (reference CLI defaults)",
     "sa-learned": "SK n=1024 learned warm start, time-to-target",
     "pt-droplet": "parallel tempering, Chimera droplet 512/001, 128 chains x 32 temperatures x 100,000 sweeps",
+    "pa-droplet": "population annealing, Chimera droplet 512/001, 16,384 replicas x 1,000 steps x 5 sweeps",
 }
 
 
@@ -794,7 +853,7 @@ def main():
         return
     if args.steps <= 0:
         args.steps = {"exhaustive36": 50, "sa-chimera": 10, "sa-sk": 5, "sa-batch": 3, "sa-n64": 50,
-                      "sa-learned": 1, "pt-droplet": 3}[args.workload]
+                      "sa-learned": 1, "pt-droplet": 3, "pa-droplet": 3}[args.workload]
     args.warmup = max(args.warmup, 3)
 
     world, rank, local, pg = dist_setup(args.gpus)
@@ -821,6 +880,8 @@ def main():
         out = bench_learned(args, ctx, pg, rank, world)
     elif args.workload == "pt-droplet":
         out = bench_pt(args, ctx, pg, rank, world)
+    elif args.workload == "pa-droplet":
+        out = bench_pa(args, ctx, pg, rank, world)
     else:
         out = bench_sa(args, ctx, pg, rank, world, args.workload)
 
@@ -836,7 +897,7 @@ def main():
                       "e2e": r["e2e"]["value"], "result": r["result"], "gpu_launches": r["gpu_launches"]}
         out["secondary"] = sec
 
-    if rank == 0 and world == 1 and args.cpu_baseline and args.workload not in ("sa-learned", "pt-droplet"):
+    if rank == 0 and world == 1 and args.cpu_baseline and args.workload not in ("sa-learned", "pt-droplet", "pa-droplet"):
         threads = os.cpu_count() or 1
         if args.workload == "exhaustive36":
             rate, sample, dt = cpu_exhaustive_rate(int_qubo(36, 0), 15.0, threads)

@@ -432,6 +432,67 @@ os_status os_pt_exchange_replay(os_ctx *ctx, uint32_t num_chains, int32_t num_te
                                 uint64_t seed, int32_t round0, int32_t num_rounds,
                                 int32_t *temps, uint64_t *swaps_accepted);
 
+/* ------------------------------------------------------------------------ */
+/* Population annealing                                                     */
+/* ------------------------------------------------------------------------ */
+
+/* No reference counterpart (benchmarks/annealing/performance.md:52-59 names
+ * population annealing beside parallel tempering as the next solver).
+ *
+ * A population of `population` replicas starts from fair-coin spins (the
+ * equilibrium at beta = 0). Step k (k = 0 .. num_steps-1) resamples the
+ * population from beta[k-1] to beta[k] (beta[-1] = 0), then runs
+ * sweeps_per_beta colour-parallel sweeps of every replica at beta[k]
+ * (physical rule). Resampling is systematic: with weights
+ * w_i = exp(-(beta[k] - beta[k-1]) (E_i - E_min)) and cumulative sums
+ * C_i = w_0 + ... + w_i, slot j takes the replica i with C_{i-1} <= (u + j) W / R
+ * < C_i (W = C_{R-1}, R = population, u one Philox draw per step), so the
+ * population size is fixed. The cumulative sums are formed in 1024 blocks
+ * of ceil(R / 1024) consecutive replicas: a running sum inside each block,
+ * plus the serial sum of the earlier blocks' totals. log_z[k] estimates
+ * ln Z(beta[k]) = n ln 2 + sum_{m <= k} ln Q_m with
+ * ln Q_m = -(beta[m] - beta[m-1]) E_min + ln(W / R) (Machta, PRE 82 (2010)). */
+typedef struct os_pa_params {
+  const double *beta;        /* num_steps inverse temperatures (host),
+                                finite and >= 0 */
+  int32_t num_steps;         /* >= 1 */
+  int32_t sweeps_per_beta;   /* sweeps of every replica per step, >= 1 */
+  uint32_t population;       /* replicas, 1 .. 65535 */
+  uint64_t seed;             /* Philox key */
+  int32_t resync_every;      /* steps between FP64 local-field resyncs
+                                (0 = one check at the end) */
+} os_pa_params;
+
+typedef struct os_pa_result {
+  char *state;               /* [n] best state any replica visited */
+  double energy;             /* its FP64 energy (reference energy function) */
+  double *log_z;             /* optional [num_steps]: ln Z estimates */
+  double *final_energies;    /* optional [population]: FP64 energies of the
+                                final population */
+  char *final_states;        /* optional [population * n] */
+  uint32_t families;         /* distinct initial replicas that still have
+                                descendants at the end */
+  double max_field_drift;    /* max |h_fp32 - h_fp64| over resyncs */
+  uint64_t attempts;         /* spin-flip attempts performed */
+  uint64_t accepted;         /* accepted flips */
+  double device_ms;          /* device time of the steps (resampling,
+                                copies, sweeps, resyncs), CUDA events */
+} os_pa_result;
+
+/* Population annealing on a sparse QUBO (CSR as for os_sa_run_sparse), with
+ * the sparse annealing kernel as the sweep; host buffers in and out. */
+os_status os_pa_run_sparse(os_ctx *ctx, const os_qubo_csr *qubo,
+                           const os_pa_params *params, os_pa_result *result);
+
+/* Resampling-only replay for verification: the resampling step of
+ * os_pa_run_sparse for step `step` on caller-given energies[population]
+ * with inverse-temperature increment dbeta. parents[population] receives
+ * each slot's parent replica and *log_q the step's ln Q. Same Philox draw as
+ * os_pa_run_sparse with that seed. */
+os_status os_pa_resample_replay(os_ctx *ctx, uint32_t population, const double *energies,
+                                double dbeta, uint64_t seed, int32_t step,
+                                int32_t *parents, double *log_q);
+
 /* Philox4x32-10 of the device generator, evaluated on the GPU for `count`
  * consecutive counters starting at ctr (ctr[0] incremented); out receives
  * 4*count words. For checking the generator against its published

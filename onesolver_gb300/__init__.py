@@ -11,9 +11,10 @@ a thin ctypes mirror of that ABI and of the reference's user-facing calls:
   (``include/simulated_annealing/annealing.hpp``);
 * :func:`linear_schedule` / :func:`geometric_schedule` -- the CLI's beta
   schedules (``app/one-solver-anneal.cpp:23-39``);
-* :func:`temper_sparse` -- parallel tempering on the sparse sweep kernel (no
-  reference counterpart; ``benchmarks/annealing/performance.md:52-59`` names
-  it as the next solver).
+* :func:`temper_sparse` / :func:`population_anneal_sparse` -- parallel
+  tempering and population annealing on the sparse sweep kernel (no reference
+  counterpart; ``benchmarks/annealing/performance.md:52-59`` names them as the
+  next solvers).
 
 There is no CPU fallback: every solver call runs on the GPU through the native
 library, and importing the library fails loudly when it has not been built.
@@ -105,6 +106,18 @@ class _PtResult(C.Structure):
                 ("attempts", C.c_uint64), ("accepted", C.c_uint64), ("device_ms", C.c_double)]
 
 
+class _PaParams(C.Structure):
+    _fields_ = [("beta", C.POINTER(C.c_double)), ("num_steps", C.c_int32), ("sweeps_per_beta", C.c_int32),
+                ("population", C.c_uint32), ("seed", C.c_uint64), ("resync_every", C.c_int32)]
+
+
+class _PaResult(C.Structure):
+    _fields_ = [("state", C.c_char_p), ("energy", C.c_double), ("log_z", C.POINTER(C.c_double)),
+                ("final_energies", C.POINTER(C.c_double)), ("final_states", C.c_char_p),
+                ("families", C.c_uint32), ("max_field_drift", C.c_double), ("attempts", C.c_uint64),
+                ("accepted", C.c_uint64), ("device_ms", C.c_double)]
+
+
 _lib: Optional[C.CDLL] = None
 
 # Every symbol of include/onesolver.h with (restype, argtypes).
@@ -165,6 +178,9 @@ SIGNATURES = {
     "os_pt_exchange_replay": (C.c_int, [_P, C.c_uint32, C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_double),
                                         C.c_uint64, C.c_int32, C.c_int32, C.POINTER(C.c_int32),
                                         C.POINTER(C.c_uint64)]),
+    "os_pa_run_sparse": (C.c_int, [_P, C.POINTER(_QuboCsr), C.POINTER(_PaParams), C.POINTER(_PaResult)]),
+    "os_pa_resample_replay": (C.c_int, [_P, C.c_uint32, C.POINTER(C.c_double), C.c_double, C.c_uint64, C.c_int32,
+                                        C.POINTER(C.c_int32), C.POINTER(C.c_double)]),
     "os_philox_sample": (C.c_int, [_P, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.c_int32,
                                    C.POINTER(C.c_uint32)]),
     "os_mpnn_create": (C.c_int, [_P, C.c_int32, C.c_int32, C.c_int32, C.c_uint64, C.POINTER(_P)]),
@@ -727,6 +743,62 @@ def pt_exchange_replay(beta: Sequence[float], energies: np.ndarray, temps: np.nd
                                        t.ctypes.data_as(C.POINTER(C.c_int32)),
                                        sw.ctypes.data_as(C.POINTER(C.c_uint64))))
     return t, sw[: nt - 1]
+
+
+@dataclass
+class PopulationResult:
+    state: np.ndarray            # uint8[n], best state any replica visited
+    energy: float                # its FP64 energy (reference energy function)
+    log_z: np.ndarray            # float64[num_steps], ln Z(beta[k]) estimates
+    final_energies: np.ndarray   # float64[population]
+    final_states: Optional[np.ndarray]
+    families: int                # initial replicas with descendants at the end
+    max_field_drift: float
+    attempts: int
+    accepted: int
+    device_ms: float
+
+
+def population_anneal_sparse(csr: Csr, beta: Sequence[float], *, population: int = 4096, sweeps_per_beta: int = 5,
+                             seed: int = 1234, resync_every: int = 0, ctx: Optional[Context] = None,
+                             final_states: bool = False) -> PopulationResult:
+    """Population annealing on a sparse QUBO: systematic resampling between
+    consecutive inverse temperatures (from beta = 0), then sweeps_per_beta
+    colour-parallel sweeps of every replica. No reference counterpart
+    (benchmarks/annealing/performance.md:52-59 names it as a next solver)."""
+    ctx = ctx or default_context()
+    q = csr._c()
+    b = np.ascontiguousarray(beta, dtype=np.float64)
+    n = csr.n
+    prm = _PaParams(_dptr(b), len(b), sweeps_per_beta, population, seed, resync_every)
+    state = C.create_string_buffer(n)
+    lz = np.zeros(len(b), dtype=np.float64)
+    fe = np.zeros(population, dtype=np.float64)
+    fs = C.create_string_buffer(n * population) if final_states else None
+    res = _PaResult()
+    res.state = C.cast(state, C.c_char_p)
+    res.log_z = _dptr(lz)
+    res.final_energies = _dptr(fe)
+    res.final_states = C.cast(fs, C.c_char_p) if fs is not None else None
+    _check(lib().os_pa_run_sparse(ctx.handle, C.byref(q), C.byref(prm), C.byref(res)))
+    return PopulationResult(np.frombuffer(state.raw[:n], dtype=np.uint8).copy(), res.energy, lz, fe,
+                            np.frombuffer(fs.raw[: n * population], dtype=np.uint8).reshape(population, n).copy()
+                            if fs is not None else None,
+                            int(res.families), res.max_field_drift, int(res.attempts), int(res.accepted),
+                            res.device_ms)
+
+
+def pa_resample_replay(energies: np.ndarray, dbeta: float, *, seed: int = 1234, step: int = 0,
+                       ctx: Optional[Context] = None):
+    """The resampling step of population_anneal_sparse alone, on the GPU;
+    returns (parent of each slot, ln Q)."""
+    ctx = ctx or default_context()
+    e = np.ascontiguousarray(energies, dtype=np.float64)
+    par = np.zeros(len(e), dtype=np.int32)
+    lq = C.c_double()
+    _check(lib().os_pa_resample_replay(ctx.handle, len(e), _dptr(e), dbeta, seed, step,
+                                       par.ctypes.data_as(C.POINTER(C.c_int32)), C.byref(lq)))
+    return par, lq.value
 
 
 def _batch_inputs(instances):

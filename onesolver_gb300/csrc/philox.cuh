@@ -59,6 +59,7 @@ enum : uint32_t {
   kStreamSweep = 0x2u << 28,   // acceptance uniforms (sequential sites)
   kStreamSite = 0x3u << 28,    // site index + uniform (random sites)
   kStreamExchange = 0x4u << 28,  // replica-exchange uniforms (tempering)
+  kStreamResample = 0x5u << 28,  // resampling offsets (population annealing)
 };
 
 // Uniform in (0, 1) in FP64 from one 32-bit word: (r + 0.5) * 2^-32, exact.

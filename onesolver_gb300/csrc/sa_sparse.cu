@@ -785,6 +785,305 @@ static void pt_result(PtRun &pr, os_pt_result *res) {
   res->device_ms = ms;
 }
 
+// ---------------------------------------------------------------------------
+// Population annealing (Hukushima and Iba, AIP Conf. Proc. 690 (2003);
+// Machta, PRE 82 (2010)). No counterpart in the reference, whose annealing
+// benchmark names it beside parallel tempering as the next solver
+// (benchmarks/annealing/performance.md:52-59). Between two inverse
+// temperatures the population is resampled systematically (fixed size) in
+// proportion to exp(-dbeta E); every replica then sweeps with the sparse
+// annealing kernel.
+// ---------------------------------------------------------------------------
+
+constexpr int RESAMPLE_THREADS = 1024;
+
+struct ResampleArgs {
+  const double *e;     // [R] energies of the current population
+  int R;
+  double dbeta;
+  int step;
+  uint32_t seed_lo, seed_hi;
+  double *cum;         // [R] scratch: cumulative weights
+  int *parent;         // [R] out: parent of each slot
+  double *logq;        // out: ln Q of the step
+};
+
+// One CTA. Block t of the cumulative sums covers replicas
+// [t L, min((t+1) L, R)), L = ceil(R / 1024): a running sum inside the
+// block, then the serial sum of the earlier blocks' totals added to every
+// entry, so the host oracle can form the same sums in the same order.
+__global__ void __launch_bounds__(RESAMPLE_THREADS) pa_resample_kernel(const __grid_constant__ ResampleArgs a) {
+  __shared__ double s_tot[RESAMPLE_THREADS];
+  __shared__ double s_min[RESAMPLE_THREADS / 32];
+  __shared__ double s_w;
+  const int t = threadIdx.x;
+  const int L = (a.R + RESAMPLE_THREADS - 1) / RESAMPLE_THREADS;
+  const int b0 = t * L, b1 = min(a.R, b0 + L);
+  double emin = INFINITY;
+  for (int i = b0; i < b1; ++i) emin = fmin(emin, a.e[i]);
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) emin = fmin(emin, __shfl_xor_sync(0xffffffffu, emin, off));
+  if ((t & 31) == 0) s_min[t >> 5] = emin;
+  __syncthreads();
+  emin = s_min[0];
+  for (int w = 1; w < RESAMPLE_THREADS / 32; ++w) emin = fmin(emin, s_min[w]);
+  double run = 0.0;
+  for (int i = b0; i < b1; ++i) {
+    run += exp(-a.dbeta * (a.e[i] - emin));
+    a.cum[i] = run;
+  }
+  s_tot[t] = run;
+  __syncthreads();
+  if (t == 0) {
+    double acc = 0.0;
+    for (int k = 0; k < RESAMPLE_THREADS; ++k) {
+      const double v = s_tot[k];
+      s_tot[k] = acc;  // exclusive prefix
+      acc += v;
+    }
+    s_w = acc;
+    *a.logq = __dadd_rn(__dmul_rn(-a.dbeta, emin), log(acc / a.R));
+  }
+  __syncthreads();
+  const double off = s_tot[t];
+  for (int i = b0; i < b1; ++i) a.cum[i] = off + a.cum[i];
+  __syncthreads();
+  const Philox4 p = philox4x32_10((uint32_t)a.step, 0u, 0u, kStreamResample, a.seed_lo, a.seed_hi);
+  const double u = u01_open64(p.x);
+  const double stride = s_w / a.R;
+  for (int j = t; j < a.R; j += RESAMPLE_THREADS) {
+    const double target = (u + j) * stride;
+    int lo = 0, hi = a.R - 1;  // first i with cum[i] > target, at most R - 1
+    while (lo < hi) {
+      const int mid = (lo + hi) >> 1;
+      if (a.cum[mid] > target)
+        hi = mid;
+      else
+        lo = mid + 1;
+    }
+    a.parent[j] = lo;
+  }
+}
+
+struct PaCopyArgs {
+  const int *parent;
+  int n, R;
+  const float *h;
+  const uint8_t *x, *xbest;
+  const double *e, *ebest;
+  const int *anc;
+  float *h2;
+  uint8_t *x2, *xbest2;
+  double *e2, *ebest2;
+  int *anc2;
+};
+
+// Slot j of the new population becomes a copy of replica parent[j] (fields,
+// spins, best state, energies, ancestor). One CTA per slot.
+__global__ void __launch_bounds__(128) pa_copy_kernel(const __grid_constant__ PaCopyArgs a) {
+  const int j = blockIdx.x;
+  if (j >= a.R) return;
+  const int src = a.parent[j];
+  const size_t so = (size_t)src * a.n, dst = (size_t)j * a.n;
+  for (int i = threadIdx.x; i < a.n; i += blockDim.x) {
+    a.h2[dst + i] = a.h[so + i];
+    a.x2[dst + i] = a.x[so + i];
+    a.xbest2[dst + i] = a.xbest[so + i];
+  }
+  if (threadIdx.x == 0) {
+    a.e2[j] = a.e[src];
+    a.ebest2[j] = a.ebest[src];
+    a.anc2[j] = a.anc[src];
+  }
+}
+
+__global__ void iota_kernel(int *v, int count) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < count) v[i] = i;
+}
+
+static void check_pa_params(const os_pa_params *prm) {
+  OS_REQUIRE(prm != nullptr, "null parameters");
+  OS_REQUIRE(prm->beta != nullptr && prm->num_steps >= 1, "empty beta schedule");
+  for (int k = 0; k < prm->num_steps; ++k)
+    OS_REQUIRE(std::isfinite(prm->beta[k]) && prm->beta[k] >= 0.0, "beta[%d] must be finite and >= 0", k);
+  OS_REQUIRE(prm->sweeps_per_beta >= 1, "sweeps_per_beta must be positive");
+  OS_REQUIRE(prm->population >= 1 && prm->population <= 65535, "population must be in 1 .. 65535");
+  OS_REQUIRE(prm->resync_every >= 0, "resync_every must be >= 0");
+  const long long steps = (long long)prm->num_steps * prm->sweeps_per_beta;
+  OS_REQUIRE(steps < (1ll << 31), "too many sweeps (%lld)", steps);
+}
+
+struct PaRun {
+  os_sa_plan p;                // sparse buffers of the current population; beta = the schedule
+  int K = 0, spb = 0, resync = 0;
+  std::vector<double> beta;    // host copy of the schedule
+  os::DevBuf<float> h2;        // the other population (copy target)
+  os::DevBuf<uint8_t> x2, xbest2;
+  os::DevBuf<double> e2, ebest2, cum, logq, efinal;
+  os::DevBuf<int> parent, anc, anc2;
+  cudaEvent_t ev[2] = {nullptr, nullptr};
+  ~PaRun() {
+    for (auto e : ev)
+      if (e) cudaEventDestroy(e);
+  }
+};
+
+template <class T> static void swap_buf(os::DevBuf<T> &a, os::DevBuf<T> &b) {
+  std::swap(a.ptr, b.ptr);
+  std::swap(a.count, b.count);
+}
+
+static void pa_create(PaRun &pr, os_ctx *ctx, const os_qubo_csr *q, const os_pa_params *prm) {
+  OS_REQUIRE(q != nullptr, "null QUBO");
+  check_pa_params(prm);
+  os_sa_params sp{};
+  sp.beta = prm->beta;
+  sp.num_iter = prm->num_steps;
+  sp.sweeps_per_beta = prm->sweeps_per_beta;
+  sp.num_tries = prm->population;
+  sp.seed = prm->seed;
+  sp.acceptance = OS_ACCEPT_PHYSICAL;
+  sp.site_order = OS_SITES_SEQUENTIAL;
+  sp.resync_every = 0;
+  sp.init_prob = nullptr;
+  pr.p.kind = 1;
+  os_sa_plan_common(&pr.p, ctx, &sp, q->n);
+  plan_create_sparse(&pr.p, q);
+  pr.K = prm->num_steps;
+  pr.spb = prm->sweeps_per_beta;
+  pr.resync = prm->resync_every;
+  pr.beta.assign(prm->beta, prm->beta + prm->num_steps);
+  const size_t R = prm->population, n = (size_t)q->n;
+  pr.h2.alloc(R * n);
+  pr.x2.alloc(R * n);
+  pr.xbest2.alloc(R * n);
+  pr.e2.alloc(R);
+  pr.ebest2.alloc(R);
+  pr.cum.alloc(R);
+  pr.logq.alloc(pr.K);
+  pr.efinal.alloc(R);
+  pr.parent.alloc(R);
+  pr.anc.alloc(R);
+  pr.anc2.alloc(R);
+  for (auto &e : pr.ev) OS_CUDA(cudaEventCreate(&e));
+}
+
+static void pa_execute(PaRun &pr) {
+  os_sa_plan *p = &pr.p;
+  cudaStream_t s = p->ctx->stream;
+  p->launches = 0;
+  const int n = p->n, R = p->T;
+  iota_kernel<<<(R + 127) / 128, 128, 0, s>>>(pr.anc.get(), R);
+  OS_CUDA(cudaGetLastError());
+  SparseResyncArgs r = start_sparse(p);
+  p->launches += 1;
+  ResampleArgs ra{};
+  ra.R = R;
+  ra.seed_lo = r.seed_lo;
+  ra.seed_hi = r.seed_hi;
+  ra.cum = pr.cum.get();
+  ra.parent = pr.parent.get();
+  const int cta_traj = p->traj_per_cta;
+  const int threads = p->warps * 32;
+  const size_t smem = (size_t)n * 5 * cta_traj;
+  const int grid = (R + cta_traj - 1) / cta_traj;
+  OS_CUDA(cudaEventRecord(pr.ev[0], s));
+  for (int k = 0; k < pr.K; ++k) {
+    ra.e = p->se.get();
+    ra.dbeta = pr.beta[k] - (k ? pr.beta[k - 1] : 0.0);
+    ra.step = k;
+    ra.logq = pr.logq.get() + k;
+    pa_resample_kernel<<<1, RESAMPLE_THREADS, 0, s>>>(ra);
+    OS_CUDA(cudaGetLastError());
+    PaCopyArgs ca{};
+    ca.parent = pr.parent.get();
+    ca.n = n;
+    ca.R = R;
+    ca.h = p->sh.get();
+    ca.x = p->sx.get();
+    ca.xbest = p->sxbest.get();
+    ca.e = p->se.get();
+    ca.ebest = p->sebest.get();
+    ca.anc = pr.anc.get();
+    ca.h2 = pr.h2.get();
+    ca.x2 = pr.x2.get();
+    ca.xbest2 = pr.xbest2.get();
+    ca.e2 = pr.e2.get();
+    ca.ebest2 = pr.ebest2.get();
+    ca.anc2 = pr.anc2.get();
+    pa_copy_kernel<<<R, 128, 0, s>>>(ca);
+    OS_CUDA(cudaGetLastError());
+    swap_buf(p->sh, pr.h2);
+    swap_buf(p->sx, pr.x2);
+    swap_buf(p->sxbest, pr.xbest2);
+    swap_buf(p->se, pr.e2);
+    swap_buf(p->sebest, pr.ebest2);
+    swap_buf(pr.anc, pr.anc2);
+    r.h = p->sh.get();
+    r.x = p->sx.get();
+    r.xbest = p->sxbest.get();
+    r.e = p->se.get();
+    r.ebest = p->sebest.get();
+    SparseArgs a = sweep_args(p, r);
+    a.step_begin = k * pr.spb;
+    a.step_end = a.step_begin + pr.spb;
+    sa_sparse_kernel<false><<<grid, threads, smem, s>>>(a);
+    OS_CUDA(cudaGetLastError());
+    p->launches += 3;
+    if ((pr.resync > 0 && (k + 1) % pr.resync == 0) || k + 1 == pr.K) {
+      sa_sparse_resync_kernel<<<R, 256, 0, s>>>(r);
+      OS_CUDA(cudaGetLastError());
+      ++p->launches;
+    }
+  }
+  OS_CUDA(cudaEventRecord(pr.ev[1], s));
+  finish_sparse(p);
+  sa_sparse_rescore_kernel<<<(R + 127) / 128, 128, 0, s>>>(p->row_ptr.get(), p->col.get(), p->val64.get(),
+                                                           p->diag64.get(), n, R, p->sx.get(), pr.efinal.get());
+  OS_CUDA(cudaGetLastError());
+  ++p->launches;
+}
+
+static void pa_result(PaRun &pr, os_pa_result *res) {
+  OS_REQUIRE(res != nullptr, "null result");
+  os_sa_plan *p = &pr.p;
+  OS_CUDA(cudaStreamSynchronize(p->ctx->stream));
+  const int R = p->T, n = p->n;
+  std::vector<double> e(R);
+  OS_CUDA(cudaMemcpy(e.data(), p->e64.get(), sizeof(double) * R, cudaMemcpyDeviceToHost));
+  std::vector<unsigned long long> acc(R);
+  OS_CUDA(cudaMemcpy(acc.data(), p->accepted.get(), sizeof(unsigned long long) * R, cudaMemcpyDeviceToHost));
+  unsigned long long drift_bits = 0;
+  OS_CUDA(cudaMemcpy(&drift_bits, p->drift.get(), sizeof drift_bits, cudaMemcpyDeviceToHost));
+  std::vector<int> anc(R);
+  OS_CUDA(cudaMemcpy(anc.data(), pr.anc.get(), sizeof(int) * R, cudaMemcpyDeviceToHost));
+  const int best = argmin_first(e);
+  if (res->state) OS_CUDA(cudaMemcpy(res->state, p->states.get() + (size_t)best * n, n, cudaMemcpyDeviceToHost));
+  res->energy = e[best];
+  if (res->log_z) {
+    std::vector<double> lq(pr.K);
+    OS_CUDA(cudaMemcpy(lq.data(), pr.logq.get(), sizeof(double) * pr.K, cudaMemcpyDeviceToHost));
+    double z = n * std::log(2.0);
+    for (int k = 0; k < pr.K; ++k) res->log_z[k] = (z += lq[k]);
+  }
+  if (res->final_energies)
+    OS_CUDA(cudaMemcpy(res->final_energies, pr.efinal.get(), sizeof(double) * R, cudaMemcpyDeviceToHost));
+  if (res->final_states) OS_CUDA(cudaMemcpy(res->final_states, p->sx.get(), (size_t)R * n, cudaMemcpyDeviceToHost));
+  std::sort(anc.begin(), anc.end());
+  res->families = (uint32_t)(std::unique(anc.begin(), anc.end()) - anc.begin());
+  double drift;
+  std::memcpy(&drift, &drift_bits, sizeof drift);
+  res->max_field_drift = drift;
+  res->attempts = (unsigned long long)p->steps * (unsigned long long)n * (unsigned long long)R;
+  unsigned long long total = 0;
+  for (auto v : acc) total += v;
+  res->accepted = total;
+  float ms = 0.f;
+  OS_CUDA(cudaEventElapsedTime(&ms, pr.ev[0], pr.ev[1]));
+  res->device_ms = ms;
+}
+
 }  // namespace sa
 }  // namespace os
 
@@ -893,6 +1192,54 @@ os_status os_pt_exchange_replay(os_ctx *ctx, uint32_t num_chains, int32_t num_te
     if (swaps_accepted && num_temps > 1)
       OS_CUDA(cudaMemcpyAsync(swaps_accepted, sw.get(), sizeof(unsigned long long) * (num_temps - 1),
                               cudaMemcpyDeviceToHost, s));
+    OS_CUDA(cudaStreamSynchronize(s));
+  });
+}
+
+
+os_status os_pa_run_sparse(os_ctx *ctx, const os_qubo_csr *qubo, const os_pa_params *params,
+                           os_pa_result *result) {
+  return guard([&] {
+    activate(ctx);
+    OS_REQUIRE(result != nullptr, "null result");
+    PaRun pr;
+    pa_create(pr, ctx, qubo, params);
+    pa_execute(pr);
+    pa_result(pr, result);
+  });
+}
+
+os_status os_pa_resample_replay(os_ctx *ctx, uint32_t population, const double *energies, double dbeta,
+                                uint64_t seed, int32_t step, int32_t *parents, double *log_q) {
+  return guard([&] {
+    activate(ctx);
+    OS_REQUIRE(energies && parents && log_q, "null argument");
+    OS_REQUIRE(population >= 1 && population <= (1u << 24), "population must be in 1 .. 2^24");
+    OS_REQUIRE(std::isfinite(dbeta), "dbeta must be finite");
+    OS_REQUIRE(step >= 0, "step must be >= 0");
+    for (uint32_t i = 0; i < population; ++i) OS_REQUIRE(std::isfinite(energies[i]), "energies[%u] not finite", i);
+    cudaStream_t s = ctx->stream;
+    DevBuf<double> e, cum, lq;
+    DevBuf<int> par;
+    e.alloc(population);
+    cum.alloc(population);
+    lq.alloc(1);
+    par.alloc(population);
+    OS_CUDA(cudaMemcpyAsync(e.get(), energies, sizeof(double) * population, cudaMemcpyHostToDevice, s));
+    ResampleArgs ra{};
+    ra.e = e.get();
+    ra.R = (int)population;
+    ra.dbeta = dbeta;
+    ra.step = step;
+    ra.seed_lo = (uint32_t)seed;
+    ra.seed_hi = (uint32_t)(seed >> 32);
+    ra.cum = cum.get();
+    ra.parent = par.get();
+    ra.logq = lq.get();
+    pa_resample_kernel<<<1, RESAMPLE_THREADS, 0, s>>>(ra);
+    OS_CUDA(cudaGetLastError());
+    OS_CUDA(cudaMemcpyAsync(parents, par.get(), sizeof(int) * population, cudaMemcpyDeviceToHost, s));
+    OS_CUDA(cudaMemcpyAsync(log_q, lq.get(), sizeof(double), cudaMemcpyDeviceToHost, s));
     OS_CUDA(cudaStreamSynchronize(s));
   });
 }

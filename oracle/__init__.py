@@ -70,6 +70,8 @@ def lib() -> C.CDLL:
         L.orc_philox4x32_10.restype = None
         L.orc_pt_exchange.argtypes = [C.c_int, C.c_int, _D, _D, C.c_uint64, C.c_int, C.c_int, _I, _U64]
         L.orc_pt_exchange.restype = None
+        L.orc_pa_resample.argtypes = [C.c_int, _D, C.c_double, C.c_uint64, C.c_int, _I, _D]
+        L.orc_pa_resample.restype = None
         L.orc_solution_csv.argtypes = [C.c_char_p, C.c_int, C.c_double, C.c_char_p, C.c_int]
         L.orc_solution_csv.restype = C.c_int
         _lib = L
@@ -200,6 +202,15 @@ def pt_exchange(beta, energies, seed: int, round0: int, rounds: int, temps):
     lib().orc_pt_exchange(chains, nt, _d(b), _d(e), seed, round0, rounds,
                           t.ctypes.data_as(_I), sw.ctypes.data_as(_U64))
     return t, sw[: nt - 1]
+
+
+def pa_resample(energies, dbeta: float, seed: int, step: int):
+    """One systematic resampling step; returns (parent of each slot, ln Q)."""
+    e = np.ascontiguousarray(energies, dtype=np.float64)
+    par = np.zeros(len(e), dtype=np.int32)
+    lq = C.c_double()
+    lib().orc_pa_resample(len(e), _d(e), dbeta, seed, step, par.ctypes.data_as(_I), C.byref(lq))
+    return par, lq.value
 
 
 def solution_csv(state, energy_value: float) -> str:

@@ -467,4 +467,53 @@ void orc_pt_exchange(int chains, int nt, const double *beta, const double *e, ui
   }
 }
 
+
+// Systematic resampling step of population annealing (Hukushima and Iba,
+// 2003; Machta, PRE 82 (2010)). Not in the reference (its annealing benchmark
+// names population annealing as a next solver,
+// benchmarks/annealing/performance.md:52-59): the project's own statement of
+// the rule the GPU library implements. Weights w_i = exp(-dbeta (E_i - E_min));
+// cumulative sums in 1024 blocks of L = ceil(R / 1024) consecutive replicas
+// (running sum inside a block, plus the serial sum of the earlier blocks'
+// totals); W = the sum of all block totals in order; u = (w + 1/2) 2^-32 from
+// the first word of Philox4x32-10 at counter (step, 0, 0, 5 << 28); slot j
+// takes the first i (at most R - 1) with cum_i > (u + j) (W / R);
+// ln Q = (-dbeta E_min) + ln(W / R).
+void orc_pa_resample(int R, const double *e, double dbeta, uint64_t seed, int step, int *parent, double *log_q) {
+  const int B = 1024;
+  const int L = (R + B - 1) / B;
+  double emin = INFINITY;
+  for (int i = 0; i < R; ++i) emin = std::fmin(emin, e[i]);
+  std::vector<double> cum(R), tot(B, 0.0);
+  for (int b = 0; b < B; ++b) {
+    double run = 0.0;
+    for (int i = b * L; i < std::min(R, (b + 1) * L); ++i) {
+      const double x = -dbeta * (e[i] - emin);
+      run += std::exp(x);
+      cum[i] = run;
+    }
+    tot[b] = run;
+  }
+  double acc = 0.0;
+  for (int b = 0; b < B; ++b) {
+    const double off = acc;
+    acc += tot[b];
+    for (int i = b * L; i < std::min(R, (b + 1) * L); ++i) cum[i] = off + cum[i];
+  }
+  const double m = -dbeta * emin;
+  const double lg = std::log(acc / R);
+  *log_q = m + lg;
+  const uint32_t key[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)};
+  const uint32_t ctr[4] = {(uint32_t)step, 0u, 0u, 5u << 28};
+  uint32_t w[4];
+  philox4x32_10(ctr, key, w);
+  const double u = ((double)w[0] + 0.5) * 0x1.0p-32;
+  const double stride = acc / R;
+  for (int j = 0; j < R; ++j) {
+    const double target = (u + j) * stride;
+    const int i = (int)(std::upper_bound(cum.begin(), cum.end(), target) - cum.begin());
+    parent[j] = std::min(i, R - 1);
+  }
+}
+
 }  // extern "C"

@@ -1,0 +1,147 @@
+"""Population annealing on the sparse sweep kernel.
+
+No reference counterpart: the reference's annealing benchmark names
+population annealing beside parallel tempering as the next solver
+(benchmarks/annealing/performance.md:52-59).
+
+CPU tests pin the oracle's resampling step (a second, pure-Python
+transcription; the systematic-resampling count bound). GPU tests check:
+  * the device resampling step against the oracle, bit for bit, through
+    os_pa_resample_replay;
+  * the free-energy estimates ln Z(beta_k) against exact enumeration of a
+    small instance;
+  * the final population's mean energy against the exact Boltzmann mean;
+  * every returned state re-scores to the reported FP64 energy.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+import pytest
+
+from tests.test_pt import _all_energies, _random_sparse_ising
+
+
+def _py_resample(e, dbeta, seed, step, philox):
+    """Independent transcription of the resampling rule over Python floats."""
+    R, B = len(e), 1024
+    L = (R + B - 1) // B
+    emin = min(e)
+    cum = [0.0] * R
+    acc = 0.0
+    for b in range(B):
+        run = 0.0
+        for i in range(b * L, min(R, (b + 1) * L)):
+            run += math.exp(-dbeta * (e[i] - emin))
+            cum[i] = run
+        off = acc
+        acc += run
+        for i in range(b * L, min(R, (b + 1) * L)):
+            cum[i] = off + cum[i]
+    w = philox([step, 0, 0, 5 << 28], [seed & 0xFFFFFFFF, seed >> 32])[0]
+    u = (w + 0.5) * 2.0 ** -32
+    stride = acc / R
+    par = []
+    for j in range(R):
+        t = (u + j) * stride
+        lo, hi = 0, R - 1
+        while lo < hi:
+            mid = (lo + hi) // 2
+            if cum[mid] > t:
+                hi = mid
+            else:
+                lo = mid + 1
+        par.append(lo)
+    return np.array(par, dtype=np.int32), (-dbeta * emin) + math.log(acc / R)
+
+
+def test_oracle_resample_matches_python_transcription(orc):
+    rng = np.random.default_rng(0)
+    for R, dbeta in [(1, 0.3), (7, 0.0), (1500, 0.4), (3000, 2.5)]:
+        e = np.round(rng.normal(0, 4, R), 3)
+        p1, l1 = orc.pa_resample(e, dbeta, 17, 3)
+        p2, l2 = _py_resample(e.tolist(), dbeta, 17, 3, orc.philox)
+        assert np.array_equal(p1, p2) and l1 == l2
+
+
+def test_oracle_resample_rule(orc):
+    # Equal weights: every slot keeps its own replica, ln Q = 0.
+    p, lq = orc.pa_resample(np.arange(50, dtype=np.float64), 0.0, 1, 0)
+    assert p.tolist() == list(range(50)) and lq == 0.0
+    # Systematic resampling: replica i gets floor or ceil of R w_i / W copies.
+    rng = np.random.default_rng(3)
+    e = rng.normal(0, 3, 4000)
+    p, lq = orc.pa_resample(e, 0.7, 9, 2)
+    w = np.exp(-0.7 * (e - e.min()))
+    expect = len(e) * w / w.sum()
+    counts = np.bincount(p, minlength=len(e))
+    assert (np.abs(counts - expect) < 1 + 1e-9).all()
+    assert (np.diff(p) >= 0).all()
+    assert lq == pytest.approx(-0.7 * e.min() + math.log(w.mean()), rel=1e-12)
+
+
+# ---------------------------------------------------------------------------
+# GPU
+# ---------------------------------------------------------------------------
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("R,dbeta,step", [(1, 0.5, 0), (1000, 0.0, 4), (4097, 0.8, 11), (70000, 3.0, 2)])
+def test_resample_replay_bit_exact(native, orc, ctx, R, dbeta, step):
+    e = np.round(np.random.default_rng(R).normal(0, 5, R), 4)
+    pg, lg = native.pa_resample_replay(e, dbeta, seed=23, step=step, ctx=ctx)
+    po, lo = orc.pa_resample(e, dbeta, 23, step)
+    assert np.array_equal(pg, po)
+    assert lg == pytest.approx(lo, rel=1e-13, abs=1e-13)
+
+
+@pytest.mark.gpu
+def test_free_energy_and_final_population_match_enumeration(native, orc, ctx):
+    f = _random_sparse_ising(14, 3, 2)
+    allE = _all_energies(f)
+    beta = np.linspace(0.02, 1.0, 50)
+    R = 20000
+    res = native.population_anneal_sparse(native.Csr.from_dense(f), beta, population=R, sweeps_per_beta=2,
+                                          seed=4, ctx=ctx, final_states=True)
+    emin = allE.min()
+    exact = np.array([-b * emin + math.log(np.exp(-b * (allE - emin)).sum()) for b in beta])
+    assert np.abs(res.log_z - exact).max() < 0.05, np.abs(res.log_z - exact).max()
+    fe = orc.energy_batch(f, res.final_states)
+    assert np.array_equal(fe, res.final_energies)
+    w = np.exp(-beta[-1] * (allE - emin))
+    w /= w.sum()
+    mean = float(w @ allE)
+    sd = math.sqrt(float(w @ (allE - mean) ** 2))
+    assert 1 <= res.families <= R
+    assert abs(res.final_energies.mean() - mean) < 5 * sd / math.sqrt(res.families) + 1e-9
+    assert res.energy == pytest.approx(orc.energy(f, res.state), rel=1e-9, abs=0)
+    assert res.energy >= emin and res.attempts == R * 50 * 2 * 14
+
+
+@pytest.mark.gpu
+def test_population_annealing_rejects_bad_arguments(native, ctx):
+    from tests.test_sa_gpu import chimera_ising
+    csr = native.Csr.from_dense(chimera_ising(1, 0))
+    with pytest.raises(native.OneSolverError, match="population"):
+        native.population_anneal_sparse(csr, [1.0], population=0, ctx=ctx)
+    with pytest.raises(native.OneSolverError, match="population"):
+        native.population_anneal_sparse(csr, [1.0], population=70000, ctx=ctx)
+    with pytest.raises(native.OneSolverError, match="finite"):
+        native.population_anneal_sparse(csr, [1.0, float("nan")], ctx=ctx)
+    with pytest.raises(native.OneSolverError, match="finite"):
+        native.pa_resample_replay(np.array([0.0, np.inf]), 0.5, ctx=ctx)
+
+
+@pytest.mark.gpu
+def test_droplet_128_reaches_tensor_network_ground_state(native, orc, ctx, golden_chimera):
+    """Droplet 128/001 (reference best SA -221.573, tensor-network ground
+    state -235.867): 8,192 replicas, 300 steps of linear beta 0.05 -> 3.0 with
+    5 sweeps each."""
+    from tests.conftest import GOLDEN
+    g = golden_chimera["128"]
+    f = native.Model.load(GOLDEN / g["file"]).flatten()
+    res = native.population_anneal_sparse(native.Csr.from_dense(f), np.linspace(0.05, 3.0, 300), population=8192,
+                                          sweeps_per_beta=5, resync_every=50, seed=5, ctx=ctx)
+    assert res.energy == pytest.approx(orc.energy(f, res.state), rel=1e-9, abs=0)
+    assert abs(res.energy - g["tn_ground_qubo"]) < 1e-6, res.energy
+    assert res.max_field_drift < 1e-3
