@@ -766,7 +766,7 @@ CONFIG_NAMES = {
 
 
 PROFILE_CASES = ("exhaustive32", "exhaustive36", "sa-sk1024", "sa-batch48", "sa-batch128x256", "sa-chimera",
-                 "mpnn-predict1024", "pt-droplet512")
+                 "mpnn-predict1024", "pt-droplet512", "pa-droplet512")
 
 
 def profile_case(name: str, ctx) -> None:
@@ -800,6 +800,14 @@ def profile_case(name: str, ctx) -> None:
         csr = osg.Csr.from_dense(osg.Model.load(ROOT / "tests" / "golden" / g["file"]).flatten())
         r = osg.temper_sparse(csr, np.geomspace(0.05, 3.0, 32), num_chains=128, num_rounds=20, sweeps_per_round=5,
                               resync_every=200, ctx=ctx)
+        torch.cuda.synchronize()
+        print(json.dumps({"profile_case": name, "energy": r.energy, "device_ms": r.device_ms}))
+        return
+    elif name == "pa-droplet512":
+        g = json.loads((ROOT / "tests" / "golden" / "chimera_golden.json").read_text())["512"]
+        csr = osg.Csr.from_dense(osg.Model.load(ROOT / "tests" / "golden" / g["file"]).flatten())
+        r = osg.population_anneal_sparse(csr, np.linspace(0.05, 3.0, 1000)[:20], population=16384,
+                                         sweeps_per_beta=5, resync_every=100, ctx=ctx)
         torch.cuda.synchronize()
         print(json.dumps({"profile_case": name, "energy": r.energy, "device_ms": r.device_ms}))
         return

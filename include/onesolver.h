@@ -449,7 +449,8 @@ os_status os_pt_exchange_replay(os_ctx *ctx, uint32_t num_chains, int32_t num_te
  * < C_i (W = C_{R-1}, R = population, u one Philox draw per step), so the
  * population size is fixed. The cumulative sums are formed in 1024 blocks
  * of ceil(R / 1024) consecutive replicas: a running sum inside each block,
- * plus the serial sum of the earlier blocks' totals. log_z[k] estimates
+ * plus the block's offset (the block totals in 32 groups of 32, each group
+ * summed in order, then the group totals in order). log_z[k] estimates
  * ln Z(beta[k]) = n ln 2 + sum_{m <= k} ln Q_m with
  * ln Q_m = -(beta[m] - beta[m-1]) E_min + ln(W / R) (Machta, PRE 82 (2010)). */
 typedef struct os_pa_params {

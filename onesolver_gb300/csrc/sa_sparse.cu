@@ -808,13 +808,31 @@ struct ResampleArgs {
   double *logq;        // out: ln Q of the step
 };
 
+// Slots j with (u + j) * stride < c: a prefix of 0 .. R (the targets grow
+// with j), found from an estimate and corrected with the same comparisons a
+// search over the targets would make.
+__device__ __forceinline__ int slots_below(double c, double u, double stride, int R) {
+  double q = c / stride - u;
+  int j = q <= 0.0 ? 0 : (q >= (double)R ? R : (int)ceil(q));
+  while (j > 0 && (u + (j - 1)) * stride >= c) --j;
+  while (j < R && (u + j) * stride < c) ++j;
+  return j;
+}
+
 // One CTA. Block t of the cumulative sums covers replicas
 // [t L, min((t+1) L, R)), L = ceil(R / 1024): a running sum inside the
-// block, then the serial sum of the earlier blocks' totals added to every
-// entry, so the host oracle can form the same sums in the same order.
+// block, plus the block's offset. Offsets: the 1,024 block totals form 32
+// groups of 32; lane g of warp 0 sums group g's totals in order (its
+// exclusive prefixes are the in-group offsets), lane 0 then sums the 32 group
+// totals in order (the group offsets); offset = group offset + in-group
+// offset, and W = the last group offset + the last group total. The host
+// oracle forms the same sums in the same order. Replica i then owns the slots
+// [slots_below(cum[i-1]), slots_below(cum[i])) (the last replica also every
+// slot above), which is the first-i-with-cum[i]-above-the-target rule.
 __global__ void __launch_bounds__(RESAMPLE_THREADS) pa_resample_kernel(const __grid_constant__ ResampleArgs a) {
   __shared__ double s_tot[RESAMPLE_THREADS];
   __shared__ double s_min[RESAMPLE_THREADS / 32];
+  __shared__ double s_goff[32];
   __shared__ double s_w;
   const int t = threadIdx.x;
   const int L = (a.R + RESAMPLE_THREADS - 1) / RESAMPLE_THREADS;
@@ -834,34 +852,37 @@ __global__ void __launch_bounds__(RESAMPLE_THREADS) pa_resample_kernel(const __g
   }
   s_tot[t] = run;
   __syncthreads();
-  if (t == 0) {
-    double acc = 0.0;
-    for (int k = 0; k < RESAMPLE_THREADS; ++k) {
-      const double v = s_tot[k];
-      s_tot[k] = acc;  // exclusive prefix
-      acc += v;
+  if (t < 32) {
+    double g = 0.0;
+    for (int k = 0; k < 32; ++k) {
+      const double v = s_tot[32 * t + k];
+      s_tot[32 * t + k] = g;  // exclusive prefix inside the group
+      g += v;
     }
-    s_w = acc;
-    *a.logq = __dadd_rn(__dmul_rn(-a.dbeta, emin), log(acc / a.R));
+    s_goff[t] = g;
+    __syncwarp();
+    if (t == 0) {
+      double acc = 0.0;
+      for (int k = 0; k < 32; ++k) {
+        const double v = s_goff[k];
+        s_goff[k] = acc;
+        acc += v;
+      }
+      s_w = acc;
+      *a.logq = __dadd_rn(__dmul_rn(-a.dbeta, emin), log(acc / a.R));
+    }
   }
   __syncthreads();
-  const double off = s_tot[t];
+  const double off = s_goff[t >> 5] + s_tot[t];
   for (int i = b0; i < b1; ++i) a.cum[i] = off + a.cum[i];
   __syncthreads();
   const Philox4 p = philox4x32_10((uint32_t)a.step, 0u, 0u, kStreamResample, a.seed_lo, a.seed_hi);
   const double u = u01_open64(p.x);
   const double stride = s_w / a.R;
-  for (int j = t; j < a.R; j += RESAMPLE_THREADS) {
-    const double target = (u + j) * stride;
-    int lo = 0, hi = a.R - 1;  // first i with cum[i] > target, at most R - 1
-    while (lo < hi) {
-      const int mid = (lo + hi) >> 1;
-      if (a.cum[mid] > target)
-        hi = mid;
-      else
-        lo = mid + 1;
-    }
-    a.parent[j] = lo;
+  int j = b0 == 0 || b0 >= a.R ? 0 : slots_below(a.cum[b0 - 1], u, stride, a.R);
+  for (int i = b0; i < b1; ++i) {
+    const int j1 = i == a.R - 1 ? a.R : slots_below(a.cum[i], u, stride, a.R);
+    for (; j < j1; ++j) a.parent[j] = i;
   }
 }
 

@@ -474,8 +474,10 @@ void orc_pt_exchange(int chains, int nt, const double *beta, const double *e, ui
 // benchmarks/annealing/performance.md:52-59): the project's own statement of
 // the rule the GPU library implements. Weights w_i = exp(-dbeta (E_i - E_min));
 // cumulative sums in 1024 blocks of L = ceil(R / 1024) consecutive replicas
-// (running sum inside a block, plus the serial sum of the earlier blocks'
-// totals); W = the sum of all block totals in order; u = (w + 1/2) 2^-32 from
+// (running sum inside a block, plus the block's offset: the block totals form
+// 32 groups of 32, each group summed in order, the group totals summed in
+// order; offset = earlier groups' sum + earlier blocks of the group);
+// W = the sum of the group totals; u = (w + 1/2) 2^-32 from
 // the first word of Philox4x32-10 at counter (step, 0, 0, 5 << 28); slot j
 // takes the first i (at most R - 1) with cum_i > (u + j) (W / R);
 // ln Q = (-dbeta E_min) + ln(W / R).
@@ -494,10 +496,25 @@ void orc_pa_resample(int R, const double *e, double dbeta, uint64_t seed, int st
     }
     tot[b] = run;
   }
+  // Offsets: 32 groups of 32 block totals, each summed in order, then the
+  // group totals in order.
+  std::vector<double> pre(B), goff(32);
+  for (int g = 0; g < 32; ++g) {
+    double run = 0.0;
+    for (int k = 0; k < 32; ++k) {
+      pre[32 * g + k] = run;
+      run += tot[32 * g + k];
+    }
+    goff[g] = run;
+  }
   double acc = 0.0;
+  for (int g = 0; g < 32; ++g) {
+    const double v = goff[g];
+    goff[g] = acc;
+    acc += v;
+  }
   for (int b = 0; b < B; ++b) {
-    const double off = acc;
-    acc += tot[b];
+    const double off = goff[b / 32] + pre[b];
     for (int i = b * L; i < std::min(R, (b + 1) * L); ++i) cum[i] = off + cum[i];
   }
   const double m = -dbeta * emin;

@@ -29,16 +29,27 @@ def _py_resample(e, dbeta, seed, step, philox):
     L = (R + B - 1) // B
     emin = min(e)
     cum = [0.0] * R
-    acc = 0.0
+    tot = []
     for b in range(B):
         run = 0.0
         for i in range(b * L, min(R, (b + 1) * L)):
             run += math.exp(-dbeta * (e[i] - emin))
             cum[i] = run
-        off = acc
-        acc += run
+        tot.append(run)
+    pre, gsum = [], []
+    for g in range(32):
+        run = 0.0
+        for k in range(32):
+            pre.append(run)
+            run += tot[32 * g + k]
+        gsum.append(run)
+    goff, acc = [], 0.0
+    for g in range(32):
+        goff.append(acc)
+        acc += gsum[g]
+    for b in range(B):
         for i in range(b * L, min(R, (b + 1) * L)):
-            cum[i] = off + cum[i]
+            cum[i] = (goff[b // 32] + pre[b]) + cum[i]
     w = philox([step, 0, 0, 5 << 28], [seed & 0xFFFFFFFF, seed >> 32])[0]
     u = (w + 0.5) * 2.0 ** -32
     stride = acc / R
