@@ -795,7 +795,8 @@ static void pt_result(PtRun &pr, os_pt_result *res) {
 // annealing kernel.
 // ---------------------------------------------------------------------------
 
-constexpr int RESAMPLE_THREADS = 1024;
+constexpr int RESAMPLE_BLOCKS = 1024;  // blocks of the cumulative sums (part of the definition)
+constexpr int RESAMPLE_CTA = 32;       // threads per CTA of the resampling kernels (one block each)
 
 struct ResampleArgs {
   const double *e;     // [R] energies of the current population
@@ -803,60 +804,79 @@ struct ResampleArgs {
   double dbeta;
   int step;
   uint32_t seed_lo, seed_hi;
-  double *cum;         // [R] scratch: cumulative weights
+  double *cum;         // [R] scratch: running sums inside each block
+  double *tot;         // [RESAMPLE_BLOCKS] scratch: block totals
+  double *emin;        // [1] scratch: minimum energy
   int *parent;         // [R] out: parent of each slot
   double *logq;        // out: ln Q of the step
 };
 
+// Resampling, part 0: the population's minimum energy (one CTA).
+__global__ void __launch_bounds__(1024) pa_min_kernel(const __grid_constant__ ResampleArgs a) {
+  __shared__ double s_min[32];
+  double m = INFINITY;
+  for (int i = threadIdx.x; i < a.R; i += blockDim.x) m = fmin(m, a.e[i]);
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) m = fmin(m, __shfl_xor_sync(0xffffffffu, m, off));
+  if ((threadIdx.x & 31) == 0) s_min[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double r = s_min[0];
+    for (int w = 1; w < (int)(blockDim.x >> 5); ++w) r = fmin(r, s_min[w]);
+    *a.emin = r;
+  }
+}
+
+// Resampling, part 1: block b (thread b of the grid) covers replicas
+// [b L, min((b+1) L, R)), L = ceil(R / 1024); its weights
+// exp(-dbeta (E_i - E_min)) are summed in order into cum (running sums) and
+// tot[b] (the block total). The work is spread over 32 CTAs because FP64
+// exp is slow on one SM.
+__global__ void __launch_bounds__(RESAMPLE_CTA) pa_weights_kernel(const __grid_constant__ ResampleArgs a) {
+  const double emin = *a.emin;
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  const int L = (a.R + RESAMPLE_BLOCKS - 1) / RESAMPLE_BLOCKS;
+  const int b0 = b * L, b1 = min(a.R, b0 + L);
+  double run = 0.0;
+  for (int i = b0; i < b1; ++i) {
+    run += exp(-a.dbeta * (a.e[i] - emin));
+    a.cum[i] = run;
+  }
+  a.tot[b] = run;
+}
+
 // Slots j with (u + j) * stride < c: a prefix of 0 .. R (the targets grow
 // with j), found from an estimate and corrected with the same comparisons a
 // search over the targets would make.
-__device__ __forceinline__ int slots_below(double c, double u, double stride, int R) {
-  double q = c / stride - u;
+__device__ __forceinline__ int slots_below(double c, double u, double stride, double inv_stride, int R) {
+  const double q = c * inv_stride - u;
   int j = q <= 0.0 ? 0 : (q >= (double)R ? R : (int)ceil(q));
   while (j > 0 && (u + (j - 1)) * stride >= c) --j;
   while (j < R && (u + j) * stride < c) ++j;
   return j;
 }
 
-// One CTA. Block t of the cumulative sums covers replicas
-// [t L, min((t+1) L, R)), L = ceil(R / 1024): a running sum inside the
-// block, plus the block's offset. Offsets: the 1,024 block totals form 32
-// groups of 32; lane g of warp 0 sums group g's totals in order (its
-// exclusive prefixes are the in-group offsets), lane 0 then sums the 32 group
-// totals in order (the group offsets); offset = group offset + in-group
-// offset, and W = the last group offset + the last group total. The host
-// oracle forms the same sums in the same order. Replica i then owns the slots
-// [slots_below(cum[i-1]), slots_below(cum[i])) (the last replica also every
-// slot above), which is the first-i-with-cum[i]-above-the-target rule.
-__global__ void __launch_bounds__(RESAMPLE_THREADS) pa_resample_kernel(const __grid_constant__ ResampleArgs a) {
-  __shared__ double s_tot[RESAMPLE_THREADS];
-  __shared__ double s_min[RESAMPLE_THREADS / 32];
+// Resampling, part 2. Offsets: the 1,024 block totals form 32 groups of 32;
+// lane g of the first warp sums group g's totals in order (its exclusive
+// prefixes are the in-group offsets), lane 0 sums the 32 group totals in order
+// (the group offsets); offset = group offset + in-group offset and W = the
+// sum of the group totals. Every CTA forms them (64 dependent adds) instead of
+// waiting for another launch. Then replica i of block b, with cumulative sum
+// C_i = offset_b + cum[i], owns the slots [slots_below(C_{i-1}),
+// slots_below(C_i)) (the last replica also every slot above): the slot takes
+// the first replica whose cumulative sum exceeds its target (u + j) W / R.
+__global__ void __launch_bounds__(RESAMPLE_CTA) pa_assign_kernel(const __grid_constant__ ResampleArgs a) {
+  __shared__ double s_pre[RESAMPLE_BLOCKS];
   __shared__ double s_goff[32];
   __shared__ double s_w;
   const int t = threadIdx.x;
-  const int L = (a.R + RESAMPLE_THREADS - 1) / RESAMPLE_THREADS;
-  const int b0 = t * L, b1 = min(a.R, b0 + L);
-  double emin = INFINITY;
-  for (int i = b0; i < b1; ++i) emin = fmin(emin, a.e[i]);
-#pragma unroll
-  for (int off = 16; off > 0; off >>= 1) emin = fmin(emin, __shfl_xor_sync(0xffffffffu, emin, off));
-  if ((t & 31) == 0) s_min[t >> 5] = emin;
-  __syncthreads();
-  emin = s_min[0];
-  for (int w = 1; w < RESAMPLE_THREADS / 32; ++w) emin = fmin(emin, s_min[w]);
-  double run = 0.0;
-  for (int i = b0; i < b1; ++i) {
-    run += exp(-a.dbeta * (a.e[i] - emin));
-    a.cum[i] = run;
-  }
-  s_tot[t] = run;
+  for (int k = t; k < RESAMPLE_BLOCKS; k += blockDim.x) s_pre[k] = a.tot[k];
   __syncthreads();
   if (t < 32) {
     double g = 0.0;
     for (int k = 0; k < 32; ++k) {
-      const double v = s_tot[32 * t + k];
-      s_tot[32 * t + k] = g;  // exclusive prefix inside the group
+      const double v = s_pre[32 * t + k];
+      s_pre[32 * t + k] = g;
       g += v;
     }
     s_goff[t] = g;
@@ -869,21 +889,39 @@ __global__ void __launch_bounds__(RESAMPLE_THREADS) pa_resample_kernel(const __g
         acc += v;
       }
       s_w = acc;
-      *a.logq = __dadd_rn(__dmul_rn(-a.dbeta, emin), log(acc / a.R));
     }
   }
   __syncthreads();
-  const double off = s_goff[t >> 5] + s_tot[t];
-  for (int i = b0; i < b1; ++i) a.cum[i] = off + a.cum[i];
-  __syncthreads();
+  const double W = s_w;
+  if (blockIdx.x == 0 && t == 0) {
+    const double emin_term = __dmul_rn(-a.dbeta, *a.emin);
+    *a.logq = __dadd_rn(emin_term, log(W / a.R));
+  }
+  const int b = blockIdx.x * blockDim.x + t;
+  const int L = (a.R + RESAMPLE_BLOCKS - 1) / RESAMPLE_BLOCKS;
+  const int b0 = b * L, b1 = min(a.R, b0 + L);
+  if (b0 >= b1) return;
   const Philox4 p = philox4x32_10((uint32_t)a.step, 0u, 0u, kStreamResample, a.seed_lo, a.seed_hi);
   const double u = u01_open64(p.x);
-  const double stride = s_w / a.R;
-  int j = b0 == 0 || b0 >= a.R ? 0 : slots_below(a.cum[b0 - 1], u, stride, a.R);
+  const double stride = W / a.R, inv = a.R / W;
+  const double off = s_goff[b >> 5] + s_pre[b];
+  // The previous block's last cumulative sum is its offset plus its total
+  // (its last running sum).
+  int j = b == 0 ? 0 : slots_below(s_goff[(b - 1) >> 5] + s_pre[b - 1] + a.tot[b - 1], u, stride, inv, a.R);
   for (int i = b0; i < b1; ++i) {
-    const int j1 = i == a.R - 1 ? a.R : slots_below(a.cum[i], u, stride, a.R);
+    const int j1 = i == a.R - 1 ? a.R : slots_below(off + a.cum[i], u, stride, inv, a.R);
     for (; j < j1; ++j) a.parent[j] = i;
   }
+}
+
+static void launch_resample(const ResampleArgs &ra, cudaStream_t s) {
+  const unsigned grid = RESAMPLE_BLOCKS / RESAMPLE_CTA;
+  pa_min_kernel<<<1, 1024, 0, s>>>(ra);
+  OS_CUDA(cudaGetLastError());
+  pa_weights_kernel<<<grid, RESAMPLE_CTA, 0, s>>>(ra);
+  OS_CUDA(cudaGetLastError());
+  pa_assign_kernel<<<grid, RESAMPLE_CTA, 0, s>>>(ra);
+  OS_CUDA(cudaGetLastError());
 }
 
 struct PaCopyArgs {
@@ -941,7 +979,7 @@ struct PaRun {
   std::vector<double> beta;    // host copy of the schedule
   os::DevBuf<float> h2;        // the other population (copy target)
   os::DevBuf<uint8_t> x2, xbest2;
-  os::DevBuf<double> e2, ebest2, cum, logq, efinal;
+  os::DevBuf<double> e2, ebest2, cum, tot, emin, logq, efinal;
   os::DevBuf<int> parent, anc, anc2;
   cudaEvent_t ev[2] = {nullptr, nullptr};
   ~PaRun() {
@@ -982,6 +1020,8 @@ static void pa_create(PaRun &pr, os_ctx *ctx, const os_qubo_csr *q, const os_pa_
   pr.e2.alloc(R);
   pr.ebest2.alloc(R);
   pr.cum.alloc(R);
+  pr.tot.alloc(RESAMPLE_BLOCKS);
+  pr.emin.alloc(1);
   pr.logq.alloc(pr.K);
   pr.efinal.alloc(R);
   pr.parent.alloc(R);
@@ -1004,6 +1044,8 @@ static void pa_execute(PaRun &pr) {
   ra.seed_lo = r.seed_lo;
   ra.seed_hi = r.seed_hi;
   ra.cum = pr.cum.get();
+  ra.tot = pr.tot.get();
+  ra.emin = pr.emin.get();
   ra.parent = pr.parent.get();
   const int cta_traj = p->traj_per_cta;
   const int threads = p->warps * 32;
@@ -1015,8 +1057,7 @@ static void pa_execute(PaRun &pr) {
     ra.dbeta = pr.beta[k] - (k ? pr.beta[k - 1] : 0.0);
     ra.step = k;
     ra.logq = pr.logq.get() + k;
-    pa_resample_kernel<<<1, RESAMPLE_THREADS, 0, s>>>(ra);
-    OS_CUDA(cudaGetLastError());
+    launch_resample(ra, s);
     PaCopyArgs ca{};
     ca.parent = pr.parent.get();
     ca.n = n;
@@ -1051,7 +1092,7 @@ static void pa_execute(PaRun &pr) {
     a.step_end = a.step_begin + pr.spb;
     sa_sparse_kernel<false><<<grid, threads, smem, s>>>(a);
     OS_CUDA(cudaGetLastError());
-    p->launches += 3;
+    p->launches += 5;
     if ((pr.resync > 0 && (k + 1) % pr.resync == 0) || k + 1 == pr.K) {
       sa_sparse_resync_kernel<<<R, 256, 0, s>>>(r);
       OS_CUDA(cudaGetLastError());
@@ -1240,10 +1281,12 @@ os_status os_pa_resample_replay(os_ctx *ctx, uint32_t population, const double *
     OS_REQUIRE(step >= 0, "step must be >= 0");
     for (uint32_t i = 0; i < population; ++i) OS_REQUIRE(std::isfinite(energies[i]), "energies[%u] not finite", i);
     cudaStream_t s = ctx->stream;
-    DevBuf<double> e, cum, lq;
+    DevBuf<double> e, cum, tot, emin, lq;
     DevBuf<int> par;
     e.alloc(population);
     cum.alloc(population);
+    tot.alloc(RESAMPLE_BLOCKS);
+    emin.alloc(1);
     lq.alloc(1);
     par.alloc(population);
     OS_CUDA(cudaMemcpyAsync(e.get(), energies, sizeof(double) * population, cudaMemcpyHostToDevice, s));
@@ -1255,10 +1298,11 @@ os_status os_pa_resample_replay(os_ctx *ctx, uint32_t population, const double *
     ra.seed_lo = (uint32_t)seed;
     ra.seed_hi = (uint32_t)(seed >> 32);
     ra.cum = cum.get();
+    ra.tot = tot.get();
+    ra.emin = emin.get();
     ra.parent = par.get();
     ra.logq = lq.get();
-    pa_resample_kernel<<<1, RESAMPLE_THREADS, 0, s>>>(ra);
-    OS_CUDA(cudaGetLastError());
+    launch_resample(ra, s);
     OS_CUDA(cudaMemcpyAsync(parents, par.get(), sizeof(int) * population, cudaMemcpyDeviceToHost, s));
     OS_CUDA(cudaMemcpyAsync(log_q, lq.get(), sizeof(double), cudaMemcpyDeviceToHost, s));
     OS_CUDA(cudaStreamSynchronize(s));
