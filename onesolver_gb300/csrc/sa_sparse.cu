@@ -291,28 +291,37 @@ __global__ void __launch_bounds__(256) sa_sparse_resync_kernel(const __grid_cons
     for (int j = threadIdx.x; j < a.n; j += blockDim.x) a.xbest[(size_t)t * a.n + j] = x[j];
 }
 
-// FP64 energy of each best state in the reference's summation order
-// (annealing.hpp:31-40): set pairs (i <= j) in row-major order; CSR columns
-// are ascending so the sparse walk adds the same non-zero terms in the same
-// order as the dense loop.
-__global__ void sa_sparse_rescore_kernel(const int *__restrict__ row_ptr, const int *__restrict__ col,
-                                         const double *__restrict__ val, const double *__restrict__ diag,
-                                         int n, int T, const uint8_t *__restrict__ xs,
-                                         double *__restrict__ out) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= T) return;
-  const uint8_t *x = xs + (size_t)t * n;
+// FP64 energy of each state (n bytes per state) under the reference's
+// energy function (annealing.hpp:31-40): the set diagonal terms and the set
+// pairs i < j. One warp per state: lane l sums rows l, l + 32, ... (each row's
+// terms in column order), and a fixed shuffle tree adds the 32 partial sums,
+// so the value differs from the serial row-major sum by rounding only.
+__global__ void __launch_bounds__(256) sa_sparse_rescore_kernel(const int *__restrict__ row_ptr,
+                                                                const int *__restrict__ col,
+                                                                const double *__restrict__ val,
+                                                                const double *__restrict__ diag, int n, int T,
+                                                                const uint8_t *__restrict__ xs,
+                                                                double *__restrict__ out) {
+  const long long w = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (w >= T) return;
+  const uint8_t *x = xs + (size_t)w * n;
   double e = 0.0;
-  for (int i = 0; i < n; ++i) {
+  for (int i = lane; i < n; i += 32) {
     if (!x[i]) continue;
-    e += diag[i];
+    double r = diag[i];
     for (int k = row_ptr[i]; k < row_ptr[i + 1]; ++k) {
       const int j = col[k];
-      if (j > i && x[j]) e += val[k];
+      if (j > i && x[j]) r += val[k];
     }
+    e += r;
   }
-  out[t] = e;
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) e += __shfl_xor_sync(0xffffffffu, e, off);
+  if (lane == 0) out[w] = e;
 }
+
+static unsigned rescore_blocks(int T) { return (unsigned)ceil_div_u64((unsigned long long)T * 32, 256); }
 
 // Colouring: BFS two-colouring when the coupling graph is bipartite,
 // otherwise greedy colouring in descending-degree order.
@@ -534,7 +543,7 @@ static void finish_sparse(os_sa_plan *p) {
   cudaStream_t s = p->ctx->stream;
   const int n = p->n, T = p->T;
   OS_CUDA(cudaMemcpyAsync(p->states.get(), p->sxbest.get(), (size_t)T * n, cudaMemcpyDeviceToDevice, s));
-  sa_sparse_rescore_kernel<<<(T + 127) / 128, 128, 0, s>>>(p->row_ptr.get(), p->col.get(), p->val64.get(),
+  sa_sparse_rescore_kernel<<<rescore_blocks(T), 256, 0, s>>>(p->row_ptr.get(), p->col.get(), p->val64.get(),
                                                            p->diag64.get(), n, T, p->states.get(),
                                                            p->e64.get());
   OS_CUDA(cudaGetLastError());
@@ -736,7 +745,7 @@ static void pt_execute(PtRun &pr) {
   }
   OS_CUDA(cudaEventRecord(pr.ev[1], s));
   finish_sparse(p);
-  sa_sparse_rescore_kernel<<<(T + 127) / 128, 128, 0, s>>>(p->row_ptr.get(), p->col.get(), p->val64.get(),
+  sa_sparse_rescore_kernel<<<rescore_blocks(T), 256, 0, s>>>(p->row_ptr.get(), p->col.get(), p->val64.get(),
                                                            p->diag64.get(), n, T, p->sx.get(), pr.efinal.get());
   OS_CUDA(cudaGetLastError());
   ++p->launches;
@@ -1101,7 +1110,7 @@ static void pa_execute(PaRun &pr) {
   }
   OS_CUDA(cudaEventRecord(pr.ev[1], s));
   finish_sparse(p);
-  sa_sparse_rescore_kernel<<<(R + 127) / 128, 128, 0, s>>>(p->row_ptr.get(), p->col.get(), p->val64.get(),
+  sa_sparse_rescore_kernel<<<rescore_blocks(R), 256, 0, s>>>(p->row_ptr.get(), p->col.get(), p->val64.get(),
                                                            p->diag64.get(), n, R, p->sx.get(), pr.efinal.get());
   OS_CUDA(cudaGetLastError());
   ++p->launches;
