@@ -1,11 +1,13 @@
-// tempering.hpp -- parallel tempering on the GPU from a QUBO model.
+// tempering.hpp -- parallel tempering and population annealing on the GPU
+// from a QUBO model.
 //
 // No counterpart in quantumz-io/oneSolver: its annealing benchmark names
 // parallel tempering as the next solver (benchmarks/annealing/
 // performance.md:52-59). pt::temper takes the same model and queue as
 // sa::anneal and returns the same qubo::Solution (the lowest-energy state any
 // replica visited, FP64 energy from the reference's energy function); it runs
-// through os_pt_run_sparse on the model's couplings in CSR form.
+// through os_pt_run_sparse on the model's couplings in CSR form. pa::anneal
+// does the same through os_pa_run_sparse.
 #ifndef ONESOLVER_TEMPERING_HPP_
 #define ONESOLVER_TEMPERING_HPP_
 
@@ -93,5 +95,37 @@ qubo::Solution temper(const qubo::QUBOModel<int, T> &instance, os::Queue &q, con
 }
 
 }  // namespace pt
+
+namespace pa {
+
+// Population annealing (os_pa_run_sparse): resampling between consecutive
+// inverse temperatures of the schedule, sweeps_per_beta sweeps per step.
+struct Options {
+  unsigned population = 16384;
+  int sweeps_per_beta = 5;
+  unsigned long long seed = 1234;
+  int resync_every = 100;        // steps between FP64 field resyncs
+};
+
+template <typename T>
+qubo::Solution anneal(const qubo::QUBOModel<int, T> &instance, os::Queue &q, const std::vector<double> &beta,
+                      const Options &opt = Options()) {
+  const pt::Csr c = pt::to_csr(instance);
+  os_qubo_csr qc{c.n, c.row_ptr.data(), c.col.data(), c.val.data(), c.diag.data()};
+  os_pa_params p{};
+  p.beta = beta.data();
+  p.num_steps = (int32_t)beta.size();
+  p.sweeps_per_beta = opt.sweeps_per_beta;
+  p.population = opt.population;
+  p.seed = opt.seed;
+  p.resync_every = opt.resync_every;
+  std::vector<char> state(c.n);
+  os_pa_result r{};
+  r.state = state.data();
+  os::check(os_pa_run_sparse(q.ctx(), &qc, &p, &r));
+  return qubo::Solution(state.begin(), state.end(), r.energy);
+}
+
+}  // namespace pa
 
 #endif  // ONESOLVER_TEMPERING_HPP_

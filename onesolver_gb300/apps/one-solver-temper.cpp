@@ -1,11 +1,13 @@
-// one-solver-temper -- parallel tempering CLI on the GPU.
+// one-solver-temper -- parallel tempering and population annealing CLI on the
+// GPU (--method pt | pa).
 //
 // No counterpart in the reference, whose annealing benchmark names parallel
-// tempering as the next solver (benchmarks/annealing/performance.md:52-59).
+// tempering and population annealing as the next solvers
+// (benchmarks/annealing/performance.md:52-59).
 // Input, output, device selection, messages and the result CSV follow
 // app/one-solver-anneal.cpp so that the two tools are interchangeable in a
 // pipeline; the schedule options become a geometric ladder of inverse
-// temperatures.
+// temperatures (pt) or a linear annealing schedule of num-temps steps (pa).
 #include <fstream>
 #include <iostream>
 
@@ -21,12 +23,14 @@ int main(int argc, char *argv[]) {
     options.add_flag("help", "produce help message");
     options.add("input", "input file");
     options.add("output", "output file");
-    options.add("num-temps", "24", "number of temperatures (replicas per chain)");
+    options.add("method", "pt", "pt (parallel tempering) or pa (population annealing)");
+    options.add("num-temps", "24", "number of temperatures (pt: replicas per chain; pa: schedule steps)");
+    options.add("population", "16384", "pa: number of replicas");
     options.add("num-chains", "32", "number of independent replica chains");
     options.add("num-rounds", "1000", "number of exchange rounds");
-    options.add("sweeps-per-round", "5", "sweeps of every replica between exchange rounds");
-    options.add("beta-min", "0.05", "smallest inverse temperature of the geometric ladder");
-    options.add("beta-max", "3", "largest inverse temperature of the geometric ladder");
+    options.add("sweeps-per-round", "5", "sweeps of every replica between exchange rounds (pa: per step)");
+    options.add("beta-min", "0.05", "smallest inverse temperature (pt: geometric ladder; pa: linear schedule)");
+    options.add("beta-max", "3", "largest inverse temperature (pt: geometric ladder; pa: linear schedule)");
     options.add("device-type", "gpu", "device type to use (gpu; cpu and host are not built)");
     options.add("seed", "1234", "random seed");
     options.add("resync-every", "100", "rounds between FP64 local-field resyncs (0 = end only)");
@@ -65,6 +69,11 @@ int main(int argc, char *argv[]) {
       std::cerr << "Invalid ladder, num-temps must be positive" << std::endl;
       return -1;
     }
+    const std::string method = options.get("method");
+    if (method != "pt" && method != "pa") {
+      std::cerr << "Unknown method: " << method << std::endl;
+      return -1;
+    }
     pt::Options opt;
     opt.num_chains = (unsigned)options.get_uint("num-chains");
     opt.num_rounds = (int)options.get_uint("num-rounds");
@@ -74,10 +83,17 @@ int main(int argc, char *argv[]) {
 
     std::cout << "Reading input from: " << input_file << std::endl;
     std::cout << "Output will be saved to: " << output_file << std::endl;
-    std::cout << "Beta ladder: " << num_temps << " geometric values in [" << beta_min << ", " << beta_max << "]"
-              << std::endl;
-    std::cout << "Chains: " << opt.num_chains << ", rounds: " << opt.num_rounds
-              << ", sweeps per round: " << opt.sweeps_per_round << std::endl;
+    if (method == "pt") {
+      std::cout << "Beta ladder: " << num_temps << " geometric values in [" << beta_min << ", " << beta_max << "]"
+                << std::endl;
+      std::cout << "Chains: " << opt.num_chains << ", rounds: " << opt.num_rounds
+                << ", sweeps per round: " << opt.sweeps_per_round << std::endl;
+    } else {
+      std::cout << "Beta schedule: " << num_temps << " linear steps in [" << beta_min << ", " << beta_max << "]"
+                << std::endl;
+      std::cout << "Population: " << options.get_uint("population") << ", sweeps per step: " << opt.sweeps_per_round
+                << std::endl;
+    }
 
     std::ifstream qubo_file(input_file);
     if (!qubo_file) {
@@ -97,7 +113,18 @@ int main(int argc, char *argv[]) {
     }
     std::cout << "Using device: " << q_ptr->device_name() << std::endl;
 
-    auto solution = pt::temper(instance, *q_ptr, pt::geometric_ladder(beta_min, beta_max, num_temps), opt);
+    qubo::Solution solution = [&] {
+      if (method == "pt") return pt::temper(instance, *q_ptr, pt::geometric_ladder(beta_min, beta_max, num_temps), opt);
+      pa::Options po;
+      po.population = (unsigned)options.get_uint("population");
+      po.sweeps_per_beta = opt.sweeps_per_round;
+      po.seed = opt.seed;
+      po.resync_every = opt.resync_every;
+      std::vector<double> schedule(num_temps);
+      for (int k = 0; k < num_temps; ++k)
+        schedule[k] = num_temps == 1 ? beta_max : beta_min + (beta_max - beta_min) * k / (double)(num_temps - 1);
+      return pa::anneal(instance, *q_ptr, schedule, po);
+    }();
     std::ofstream results_file(output_file);
     solution.save(results_file);
     results_file.close();

@@ -159,7 +159,8 @@ def temper():
 def test_temper_help_and_checks(temper, small_input, tmp_path):
     rc, out, _ = run(temper, "--help")
     assert rc == 0
-    for opt in ("--input", "--output", "--num-temps", "--num-chains", "--num-rounds", "--sweeps-per-round",
+    for opt in ("--input", "--output", "--method", "--population", "--num-temps", "--num-chains", "--num-rounds",
+                "--sweeps-per-round",
                 "--beta-min", "--beta-max", "--device-type", "--seed", "--resync-every"):
         assert opt in out
     rc, _, err = run(temper)
@@ -168,6 +169,7 @@ def test_temper_help_and_checks(temper, small_input, tmp_path):
     for args, msg in [(("--beta-min", "2", "--beta-max", "1"), "beta-min is greater than beta-max"),
                       (("--beta-min", "0"), "both ends of beta range need to be positive"),
                       (("--num-temps", "0"), "num-temps must be positive"),
+                      (("--method", "qmc"), "Unknown method: qmc"),
                       (("--device-type", "fpga"), "Unknown device type: fpga")]:
         rc, _, err = run(temper, "--input", path, "--output", tmp_path / "o.csv", *args)
         assert rc == 255 and msg in err, (args, err)
@@ -187,3 +189,17 @@ def test_temper_cli_reaches_the_droplet_ground_state(temper, tmp_path, golden_ch
     e = oracle.energy(f, np.array(bits, dtype=np.uint8))
     assert abs(e - golden_chimera["128"]["tn_ground_qubo"]) < 1e-6
     assert out.read_text().splitlines()[1].split(",")[-1] == f"{e:g}"
+
+
+@pytest.mark.gpu
+def test_temper_cli_population_annealing(temper, tmp_path, golden_chimera):
+    src = ROOT / "tests" / "golden" / "chimera_128_001.qubo"
+    f = dense_from_text(src.read_text())
+    out = tmp_path / "o.csv"
+    rc, stdout, err = run(temper, "--input", src, "--output", out, "--method", "pa", "--num-temps", "300",
+                          "--population", "8192")
+    assert rc == 0, err
+    assert "Population: 8192" in stdout
+    bits, energy, _ = read_csv(out)
+    e = oracle.energy(f, np.array(bits, dtype=np.uint8))
+    assert abs(e - golden_chimera["128"]["tn_ground_qubo"]) < 1e-6
