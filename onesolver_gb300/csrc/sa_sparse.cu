@@ -51,7 +51,18 @@ struct SparseArgs {
   double *ebest;          // [T]
   unsigned long long *accepted;
   const int *temp;        // tempering: temperature index of each trajectory into beta
+  // Population annealing: trajectory t starts from replica parent[t] of the
+  // previous population (these arrays) and is written to h, x, xbest, e,
+  // ebest; anc[t] = anc_in[parent[t]].
+  const int *parent;
+  const float *h_in;
+  const uint8_t *x_in, *xbest_in;
+  const double *e_in, *ebest_in;
+  const int *anc_in;
+  int *anc;
 };
+
+enum SweepMode : int { kAnneal = 0, kTemper = 1, kPopulation = 2 };
 
 // Neighbour updates of a warp's accepted sites, applied once the colour is
 // decided (no coupler joins two sites of one colour, so the colour's own
@@ -77,10 +88,12 @@ __device__ __forceinline__ void apply_updates(const uint32_t *__restrict__ list,
   }
 }
 
-// TEMPER = false: annealing, beta[step / spb] from the schedule. TEMPER =
-// true: parallel tempering, each trajectory at its own fixed inverse
-// temperature beta[temp[t]] for the whole launch.
-template <bool TEMPER>
+// MODE kAnneal: annealing, beta[step / spb] from the schedule. kTemper:
+// parallel tempering, each trajectory at its own fixed inverse temperature
+// beta[temp[t]] for the whole launch. kPopulation: annealing whose
+// trajectories start from their resampled parents (population annealing);
+// the copy rides on the launch's own state load.
+template <int MODE>
 __global__ void __launch_bounds__(256, 8) sa_sparse_kernel(const __grid_constant__ SparseArgs a) {
   extern __shared__ unsigned char smem[];
   const int R = a.traj_per_cta;
@@ -99,16 +112,33 @@ __global__ void __launch_bounds__(256, 8) sa_sparse_kernel(const __grid_constant
   const bool active = t < a.T;
   float *h = h_all + (size_t)slot * n;
   uint8_t *x = x_all + (size_t)slot * n;
-  if (active) {
-    for (int i = tid; i < n; i += tpt) {
-      h[i] = a.h[(size_t)t * n + i];
-      x[i] = a.x[(size_t)t * n + i];
+  if constexpr (MODE == kPopulation) {
+    const int src = active ? a.parent[t] : 0;
+    if (active) {
+      for (int i = tid; i < n; i += tpt) {
+        h[i] = a.h_in[(size_t)src * n + i];
+        x[i] = a.x_in[(size_t)src * n + i];
+        a.xbest[(size_t)t * n + i] = a.xbest_in[(size_t)src * n + i];
+      }
+      if (tid == 0) a.anc[t] = a.anc_in[src];
     }
-  }
-  if (tid == 0) {
-    s_de[slot] = 0.f;
-    s_e[slot] = active ? a.e[t] : 0.0;
-    s_eb[slot] = active ? a.ebest[t] : 0.0;
+    if (tid == 0) {
+      s_de[slot] = 0.f;
+      s_e[slot] = active ? a.e_in[src] : 0.0;
+      s_eb[slot] = active ? a.ebest_in[src] : 0.0;
+    }
+  } else {
+    if (active) {
+      for (int i = tid; i < n; i += tpt) {
+        h[i] = a.h[(size_t)t * n + i];
+        x[i] = a.x[(size_t)t * n + i];
+      }
+    }
+    if (tid == 0) {
+      s_de[slot] = 0.f;
+      s_e[slot] = active ? a.e[t] : 0.0;
+      s_eb[slot] = active ? a.ebest[t] : 0.0;
+    }
   }
   __syncthreads();
   unsigned acc = 0;
@@ -117,9 +147,9 @@ __global__ void __launch_bounds__(256, 8) sa_sparse_kernel(const __grid_constant
   const int per = coop ? 32 / a.deg_max : 0;
   const int lr = coop ? lane / a.deg_max : 0, le = coop ? lane - lr * a.deg_max : 0;
   float b_fixed = 1.f;
-  if constexpr (TEMPER) b_fixed = active ? (float)a.beta[a.temp[t]] : 1.f;
+  if constexpr (MODE == kTemper) b_fixed = active ? (float)a.beta[a.temp[t]] : 1.f;
   for (int step = a.step_begin; step < a.step_end; ++step) {
-    const float b = TEMPER ? b_fixed : (float)a.beta[step / a.spb];
+    const float b = MODE == kTemper ? b_fixed : (float)a.beta[step / a.spb];
     float de = 0.f;
     for (int c = 0; c < a.ncolors; ++c) {
       const int c0 = a.color_ptr[c], cnt = a.color_ptr[c + 1] - c0;
@@ -467,7 +497,7 @@ void plan_create_sparse(os_sa_plan *p, const os_qubo_csr *q) {
   OS_REQUIRE(per <= 200 * 1024, "sparse instance too large for shared memory (%d variables)", n);
   p->traj_per_cta = R;
   p->warps = tpt * R / 32;
-  for (auto fn : {sa_sparse_kernel<false>, sa_sparse_kernel<true>})
+  for (auto fn : {sa_sparse_kernel<kAnneal>, sa_sparse_kernel<kTemper>, sa_sparse_kernel<kPopulation>})
     OS_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)std::max<size_t>(per * R, 48 * 1024)));
 }
@@ -565,7 +595,7 @@ void execute_sparse(os_sa_plan *p) {
     a.step_begin = s0;
     a.step_end = std::min(p->steps, s0 + p->chunk);
     OS_CUDA(cudaEventRecord(p->event(2 * p->sweep_ev_used), s));
-    sa_sparse_kernel<false><<<grid, threads, smem, s>>>(a);
+    sa_sparse_kernel<kAnneal><<<grid, threads, smem, s>>>(a);
     OS_CUDA(cudaGetLastError());
     OS_CUDA(cudaEventRecord(p->event(2 * p->sweep_ev_used + 1), s));
     ++p->sweep_ev_used;
@@ -727,7 +757,7 @@ static void pt_execute(PtRun &pr) {
   for (int round = 0; round < pr.rounds; ++round) {
     a.step_begin = round * pr.spr;
     a.step_end = a.step_begin + pr.spr;
-    sa_sparse_kernel<true><<<grid, threads, smem, s>>>(a);
+    sa_sparse_kernel<kTemper><<<grid, threads, smem, s>>>(a);
     OS_CUDA(cudaGetLastError());
     ++p->launches;
     if (pr.nt > 1) {
@@ -933,38 +963,6 @@ static void launch_resample(const ResampleArgs &ra, cudaStream_t s) {
   OS_CUDA(cudaGetLastError());
 }
 
-struct PaCopyArgs {
-  const int *parent;
-  int n, R;
-  const float *h;
-  const uint8_t *x, *xbest;
-  const double *e, *ebest;
-  const int *anc;
-  float *h2;
-  uint8_t *x2, *xbest2;
-  double *e2, *ebest2;
-  int *anc2;
-};
-
-// Slot j of the new population becomes a copy of replica parent[j] (fields,
-// spins, best state, energies, ancestor). One CTA per slot.
-__global__ void __launch_bounds__(128) pa_copy_kernel(const __grid_constant__ PaCopyArgs a) {
-  const int j = blockIdx.x;
-  if (j >= a.R) return;
-  const int src = a.parent[j];
-  const size_t so = (size_t)src * a.n, dst = (size_t)j * a.n;
-  for (int i = threadIdx.x; i < a.n; i += blockDim.x) {
-    a.h2[dst + i] = a.h[so + i];
-    a.x2[dst + i] = a.x[so + i];
-    a.xbest2[dst + i] = a.xbest[so + i];
-  }
-  if (threadIdx.x == 0) {
-    a.e2[j] = a.e[src];
-    a.ebest2[j] = a.ebest[src];
-    a.anc2[j] = a.anc[src];
-  }
-}
-
 __global__ void iota_kernel(int *v, int count) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < count) v[i] = i;
@@ -1067,23 +1065,25 @@ static void pa_execute(PaRun &pr) {
     ra.step = k;
     ra.logq = pr.logq.get() + k;
     launch_resample(ra, s);
-    PaCopyArgs ca{};
-    ca.parent = pr.parent.get();
-    ca.n = n;
-    ca.R = R;
-    ca.h = p->sh.get();
-    ca.x = p->sx.get();
-    ca.xbest = p->sxbest.get();
-    ca.e = p->se.get();
-    ca.ebest = p->sebest.get();
-    ca.anc = pr.anc.get();
-    ca.h2 = pr.h2.get();
-    ca.x2 = pr.x2.get();
-    ca.xbest2 = pr.xbest2.get();
-    ca.e2 = pr.e2.get();
-    ca.ebest2 = pr.ebest2.get();
-    ca.anc2 = pr.anc2.get();
-    pa_copy_kernel<<<R, 128, 0, s>>>(ca);
+    // The sweep reads each slot's parent from the current buffers and
+    // writes the new population into the other ones, which then swap.
+    SparseArgs a = sweep_args(p, r);
+    a.parent = pr.parent.get();
+    a.h_in = p->sh.get();
+    a.x_in = p->sx.get();
+    a.xbest_in = p->sxbest.get();
+    a.e_in = p->se.get();
+    a.ebest_in = p->sebest.get();
+    a.anc_in = pr.anc.get();
+    a.h = pr.h2.get();
+    a.x = pr.x2.get();
+    a.xbest = pr.xbest2.get();
+    a.e = pr.e2.get();
+    a.ebest = pr.ebest2.get();
+    a.anc = pr.anc2.get();
+    a.step_begin = k * pr.spb;
+    a.step_end = a.step_begin + pr.spb;
+    sa_sparse_kernel<kPopulation><<<grid, threads, smem, s>>>(a);
     OS_CUDA(cudaGetLastError());
     swap_buf(p->sh, pr.h2);
     swap_buf(p->sx, pr.x2);
@@ -1096,12 +1096,7 @@ static void pa_execute(PaRun &pr) {
     r.xbest = p->sxbest.get();
     r.e = p->se.get();
     r.ebest = p->sebest.get();
-    SparseArgs a = sweep_args(p, r);
-    a.step_begin = k * pr.spb;
-    a.step_end = a.step_begin + pr.spb;
-    sa_sparse_kernel<false><<<grid, threads, smem, s>>>(a);
-    OS_CUDA(cudaGetLastError());
-    p->launches += 5;
+    p->launches += 4;
     if ((pr.resync > 0 && (k + 1) % pr.resync == 0) || k + 1 == pr.K) {
       sa_sparse_resync_kernel<<<R, 256, 0, s>>>(r);
       OS_CUDA(cudaGetLastError());
