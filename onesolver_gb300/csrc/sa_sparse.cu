@@ -150,6 +150,7 @@ __global__ void __launch_bounds__(256, 8) sa_sparse_kernel(const __grid_constant
   if constexpr (MODE == kTemper) b_fixed = active ? (float)a.beta[a.temp[t]] : 1.f;
   for (int step = a.step_begin; step < a.step_end; ++step) {
     const float b = MODE == kTemper ? b_fixed : (float)a.beta[step / a.spb];
+    const float inv_b = 1.0f / b;  // physical rule: -ln(u) * (1 / beta), no division per attempt
     float de = 0.f;
     for (int c = 0; c < a.ncolors; ++c) {
       const int c0 = a.color_ptr[c], cnt = a.color_ptr[c + 1] - c0;
@@ -172,7 +173,7 @@ __global__ void __launch_bounds__(256, 8) sa_sparse_kernel(const __grid_constant
             k = a.color_sites[c0 + idx];
             const uint32_t w = m == 0 ? r.x : m == 1 ? r.y : m == 2 ? r.z : r.w;
             const float l = __logf(u01_open(w));
-            const float theta = a.acceptance == OS_ACCEPT_REFERENCE ? -b * l : -l / b;
+            const float theta = a.acceptance == OS_ACCEPT_REFERENCE ? -b * l : -l * inv_b;
             const float loc = a.diag[k] + h[k];
             const bool xk = x[k];
             const float dE = xk ? -loc : loc;
