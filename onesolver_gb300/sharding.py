@@ -1,5 +1,6 @@
-"""Exhaustive search over several processes (one per GPU): shard assignment
-by fixed top bits and the host-side merge of the shard results.
+"""Several processes (one per GPU): exhaustive search sharded by fixed top
+bits with a host-side merge of the shard results, and replicas of the
+annealing-family solvers merged by their best state.
 
 The 2^n states split by their top k bits into 2^k contiguous shards
 (`fixed_high_bits = k`, `prefix = p` enumerates the states
@@ -94,3 +95,60 @@ def exhaustive_sharded(f: np.ndarray, solve_shard: Callable[[int, int], ShardRec
         return None
     return merge_records([ShardRecord(e, np.asarray(s, dtype=np.uint64), c, m) for e, s, c, m in gathered],
                          max_minimisers)
+
+
+# ---------------------------------------------------------------------------
+# Replicas: annealing, parallel tempering, population annealing
+# ---------------------------------------------------------------------------
+#
+# Trajectories, chains and populations are independent, so N ranks run N
+# replicas of a solve with distinct Philox keys and rank 0 keeps the best
+# state: one gather of (energy, state) per rank after the kernels finish, and
+# the first minimum in rank order, the way sa::anneal takes the first
+# minimum over its trajectories (include/simulated_annealing/annealing.hpp:
+# 134-139) when rank r holds the r-th block of them.
+
+_GOLDEN64 = 0x9E3779B97F4A7C15
+
+
+def replica_seed(seed: int, rank: int) -> int:
+    """Philox key of `rank`'s replica: distinct per rank, equal to `seed` on
+    rank 0 (so a one-rank run is the plain call)."""
+    return (seed + rank * _GOLDEN64) % (1 << 64)
+
+
+@dataclass
+class ReplicaBest:
+    energy: float
+    state: np.ndarray   # uint8[n]
+    rank: int           # rank whose replica found it
+
+
+def best_over_ranks(energy: float, state: np.ndarray, *, world: int = 1, rank: int = 0,
+                    process_group=None) -> Optional[ReplicaBest]:
+    """Gather every rank's best (energy, state) on rank 0 and return the first
+    minimum in rank order there (None on the other ranks)."""
+    state = np.asarray(state, dtype=np.uint8)
+    if world == 1:
+        return ReplicaBest(float(energy), state, 0)
+    if process_group is None:
+        raise ValueError("world > 1 needs a process group (torch.distributed)")
+    gathered = [None] * world if rank == 0 else None
+    process_group.gather_object((float(energy), state.tobytes()), gathered, dst=0)
+    if rank != 0:
+        return None
+    best = 0
+    for r in range(1, world):
+        if gathered[r][0] < gathered[best][0]:
+            best = r
+    e, s = gathered[best]
+    return ReplicaBest(e, np.frombuffer(s, dtype=np.uint8).copy(), best)
+
+
+def solve_replicas(solve: Callable[[int], tuple], seed: int, *, world: int = 1, rank: int = 0,
+                   process_group=None) -> Optional[ReplicaBest]:
+    """Run `solve(seed)` -> (energy, state) with this rank's replica seed
+    (e.g. `lambda s: (r := temper_sparse(csr, beta, seed=s)).energy, r.state`)
+    and merge on rank 0."""
+    e, state = solve(replica_seed(seed, rank))
+    return best_over_ranks(e, state, world=world, rank=rank, process_group=process_group)

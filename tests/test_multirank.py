@@ -125,3 +125,45 @@ def test_gpu_shards_of_two_ranks_merge_to_the_whole_space():
     assert merged.states_enumerated == 1 << 22
     e, count, states = oracle.exhaustive_all(f, 0, 1 << 22)
     assert merged.energy == e and merged.count == count
+
+
+def _replica_worker(rank, world, port, out_dir):
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), RANK=str(rank), WORLD_SIZE=str(world))
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        f = _int_qubo(16, 3)
+
+        def solve(seed):
+            # the oracle's free-running anneal stands in for the GPU solver
+            states, energies, _ = oracle.anneal_free(f, oracle.schedule_geometric(0.2, 3.0, 40), 8, 1,
+                                                     seed=seed % (1 << 31), acceptance=1, site_order=1)
+            k = int(np.argmin(energies))
+            return float(energies[k]), np.asarray(states[k], dtype=np.uint8)
+
+        e, s = solve(sharding.replica_seed(77, rank))
+        best = sharding.solve_replicas(solve, 77, world=world, rank=rank, process_group=dist)
+        np.savez(os.path.join(out_dir, f"rep{rank}.npz"), e=e, s=s,
+                 best_e=np.nan if best is None else best.energy,
+                 best_s=np.zeros(0, np.uint8) if best is None else best.state,
+                 best_rank=-1 if best is None else best.rank)
+    finally:
+        dist.destroy_process_group()
+
+
+def test_replicas_merge_to_the_first_minimum_over_ranks(tmp_path):
+    world = 2
+    mp.spawn(_replica_worker, args=(world, _free_port(), str(tmp_path)), nprocs=world, join=True)
+    r = [np.load(tmp_path / f"rep{k}.npz") for k in range(world)]
+    energies = [float(x["e"]) for x in r]
+    first = int(np.argmin(energies))
+    assert int(r[0]["best_rank"]) == first
+    assert float(r[0]["best_e"]) == min(energies)
+    assert np.array_equal(r[0]["best_s"], r[first]["s"])
+    assert oracle.energy(_int_qubo(16, 3), r[0]["best_s"]) == min(energies)
+    assert int(r[1]["best_rank"]) == -1
+
+
+def test_replica_seeds():
+    assert sharding.replica_seed(5, 0) == 5
+    seeds = {sharding.replica_seed(5, r) for r in range(64)}
+    assert len(seeds) == 64 and all(0 <= s < (1 << 64) for s in seeds)
