@@ -481,6 +481,9 @@ void orc_pt_exchange(int chains, int nt, const double *beta, const double *e, ui
 // the first word of Philox4x32-10 at counter (step, 0, 0, 5 << 28); slot j
 // takes the first i (at most R - 1) with cum_i > (u + j) (W / R);
 // ln Q = (-dbeta E_min) + ln(W / R).
+// Built without floating-point contraction so that every product and sum
+// rounds on its own, as the device code does (__dmul_rn / __dadd_rn there).
+__attribute__((optimize("fp-contract=off")))
 void orc_pa_resample(int R, const double *e, double dbeta, uint64_t seed, int step, int *parent, double *log_q) {
   const int B = 1024;
   const int L = (R + B - 1) / B;
