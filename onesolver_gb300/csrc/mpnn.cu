@@ -5,7 +5,7 @@
 // No reference counterpart: the reference always starts trajectories from
 // fair coins (include/simulated_annealing/annealing.hpp:91-93). Its output
 // feeds os_sa_params.init_prob; plain random-init annealing stays the
-// fallback and the judge of the energy gap.
+// fallback and the yardstick of the energy gap.
 //
 // Network (H hidden units, L message-passing layers, n spins):
 //   C^      = C / (rms(C) sqrt(n))           off-diagonal couplings, BF16

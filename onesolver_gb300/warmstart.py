@@ -13,7 +13,7 @@ the C ABI):
 5. ``time_to_target`` -- the sweep budget (and wall time) each method needs to
    come within a relative gap of a target energy.
 
-Plain random-init SA is both the fallback and the judge: targets come from
+Plain random-init SA is both the fallback and the yardstick: targets come from
 long plain runs and every comparison uses the same number of trajectories.
 """
 from __future__ import annotations
