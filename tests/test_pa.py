@@ -156,3 +156,73 @@ def test_droplet_128_reaches_tensor_network_ground_state(native, orc, ctx, golde
     assert res.energy == pytest.approx(orc.energy(f, res.state), rel=1e-9, abs=0)
     assert abs(res.energy - g["tn_ground_qubo"]) < 1e-6, res.energy
     assert res.max_field_drift < 1e-3
+
+
+def _slot_ranges(e, dbeta, seed, step, philox):
+    """The device's assignment method (pa_assign_kernel) over Python floats:
+    each replica writes itself into [slots_below(C_{i-1}), slots_below(C_i)),
+    starting every block from its predecessor's last sum (offset + total)."""
+    R, B = len(e), 1024
+    L = (R + B - 1) // B
+    emin = min(e)
+    loc, tot = [0.0] * R, [0.0] * B
+    for b in range(B):
+        run = 0.0
+        for i in range(b * L, min(R, (b + 1) * L)):
+            run += math.exp(-dbeta * (e[i] - emin))
+            loc[i] = run
+        tot[b] = run
+    pre, goff = [0.0] * B, [0.0] * 32
+    for g in range(32):
+        run = 0.0
+        for k in range(32):
+            pre[32 * g + k] = run
+            run += tot[32 * g + k]
+        goff[g] = run
+    W = 0.0
+    for g in range(32):
+        v = goff[g]
+        goff[g] = W
+        W += v
+    w = philox([step, 0, 0, 5 << 28], [seed & 0xFFFFFFFF, seed >> 32])[0]
+    u = (w + 0.5) * 2.0 ** -32
+    stride, inv = W / R, R / W
+
+    def below(c):
+        q = c * inv - u
+        j = 0 if q <= 0.0 else (R if q >= R else math.ceil(q))
+        while j > 0 and (u + (j - 1)) * stride >= c:
+            j -= 1
+        while j < R and (u + j) * stride < c:
+            j += 1
+        return j
+
+    par = [-1] * R
+    for b in range(B):
+        b0, b1 = b * L, min(R, (b + 1) * L)
+        if b0 >= b1:
+            continue
+        off = goff[b // 32] + pre[b]
+        j = 0 if b == 0 else below(goff[(b - 1) // 32] + pre[b - 1] + tot[b - 1])
+        for i in range(b0, b1):
+            j1 = R if i == R - 1 else below(off + loc[i])
+            while j < j1:
+                par[j] = i
+                j += 1
+    return np.array(par, dtype=np.int32)
+
+
+@pytest.mark.parametrize("R,dbeta,scale", [(1, 0.5, 1.0), (2, 3.0, 1.0), (5, 40.0, 10.0), (1023, 0.2, 3.0),
+                                           (1025, 9.0, 5.0), (2049, 0.0, 1.0), (3000, 60.0, 20.0)])
+def test_device_slot_range_method_equals_first_exceeding_rule(orc, R, dbeta, scale):
+    # The kernel assigns slots by ranges; the definition (and the oracle) is
+    # a search for the first cumulative sum above each target. They must give
+    # the same parents everywhere, including weights that underflow to zero
+    # (large dbeta) and ties between equal energies.
+    rng = np.random.default_rng(R)
+    e = np.round(rng.normal(0, scale, R), 1)
+    for step in (0, 7):
+        par = _slot_ranges(e.tolist(), dbeta, 31, step, orc.philox)
+        ref, _ = orc.pa_resample(e, dbeta, 31, step)
+        assert (par >= 0).all()
+        assert np.array_equal(par, ref)
