@@ -565,7 +565,7 @@ def bench_pa(args, ctx, pg, rank, world):
                    "steps_at_tn_ground": sum(abs(b - g["tn_ground_qubo"]) < 1e-6 for b in best)},
         "e2e": {"value": world * attempts / t_e2e, "unit": "attempts/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(n + 8 * K + 8 * R + 12 * R), "ms_per_step": t_e2e * 1e3},
-        "gpu_launches": (3 + 3 * K + K // resync + 2) * args.steps,
+        "gpu_launches": (3 + 4 * K + K // resync + 2) * args.steps,  # per step: min, weights, assign, sweep
         "clocks": clocks,
     }
 
