@@ -692,7 +692,8 @@ struct PtRun {
   }
 };
 
-static void pt_create(PtRun &pr, os_ctx *ctx, const os_qubo_csr *q, const os_pt_params *prm) {
+// Host-only checks of the tempering parameters (no device needed).
+static void check_pt_params(const os_qubo_csr *q, const os_pt_params *prm) {
   OS_REQUIRE(prm != nullptr && q != nullptr, "null argument");
   check_ladder(prm->beta, prm->num_temps);
   OS_REQUIRE(prm->num_chains >= 1, "num_chains must be positive");
@@ -702,6 +703,12 @@ static void pt_create(PtRun &pr, os_ctx *ctx, const os_qubo_csr *q, const os_pt_
   OS_REQUIRE(total <= 65535, "parallel tempering runs at most 65535 replicas (chains x temperatures)");
   const long long steps = (long long)prm->num_rounds * prm->sweeps_per_round;
   OS_REQUIRE(steps < (1ll << 31), "too many sweeps (%lld)", steps);
+}
+
+static void pt_create(PtRun &pr, os_ctx *ctx, const os_qubo_csr *q, const os_pt_params *prm) {
+  check_pt_params(q, prm);
+  const unsigned long long total = (unsigned long long)prm->num_chains * (unsigned long long)prm->num_temps;
+  const long long steps = (long long)prm->num_rounds * prm->sweeps_per_round;
   os_sa_params sp{};
   sp.beta = prm->beta;
   sp.num_iter = prm->num_temps;
@@ -1197,8 +1204,9 @@ os_status os_sa_run_sparse(os_ctx *ctx, const os_qubo_csr *qubo, const os_sa_par
 os_status os_pt_run_sparse(os_ctx *ctx, const os_qubo_csr *qubo, const os_pt_params *params,
                            os_pt_result *result) {
   return guard([&] {
-    activate(ctx);
+    check_pt_params(qubo, params);
     OS_REQUIRE(result != nullptr, "null result");
+    activate(ctx);
     PtRun pr;
     pt_create(pr, ctx, qubo, params);
     pt_execute(pr);
@@ -1210,7 +1218,6 @@ os_status os_pt_exchange_replay(os_ctx *ctx, uint32_t num_chains, int32_t num_te
                                 const double *energies, uint64_t seed, int32_t round0, int32_t num_rounds,
                                 int32_t *temps, uint64_t *swaps_accepted) {
   return guard([&] {
-    activate(ctx);
     check_ladder(beta, num_temps);
     OS_REQUIRE(num_chains >= 1, "num_chains must be positive");
     OS_REQUIRE(round0 >= 0 && num_rounds >= 0, "rounds must be >= 0");
@@ -1225,6 +1232,7 @@ os_status os_pt_exchange_replay(os_ctx *ctx, uint32_t num_chains, int32_t num_te
                    "temps of chain %zu is not a permutation", c);
         at[c * num_temps + k] = (int)(c * num_temps + r);
       }
+    activate(ctx);
     cudaStream_t s = ctx->stream;
     DevBuf<double> b, e;
     DevBuf<int> t, ta;
@@ -1267,8 +1275,10 @@ os_status os_pt_exchange_replay(os_ctx *ctx, uint32_t num_chains, int32_t num_te
 os_status os_pa_run_sparse(os_ctx *ctx, const os_qubo_csr *qubo, const os_pa_params *params,
                            os_pa_result *result) {
   return guard([&] {
-    activate(ctx);
+    OS_REQUIRE(qubo != nullptr, "null QUBO");
+    check_pa_params(params);
     OS_REQUIRE(result != nullptr, "null result");
+    activate(ctx);
     PaRun pr;
     pa_create(pr, ctx, qubo, params);
     pa_execute(pr);
@@ -1279,12 +1289,12 @@ os_status os_pa_run_sparse(os_ctx *ctx, const os_qubo_csr *qubo, const os_pa_par
 os_status os_pa_resample_replay(os_ctx *ctx, uint32_t population, const double *energies, double dbeta,
                                 uint64_t seed, int32_t step, int32_t *parents, double *log_q) {
   return guard([&] {
-    activate(ctx);
     OS_REQUIRE(energies && parents && log_q, "null argument");
     OS_REQUIRE(population >= 1 && population <= (1u << 24), "population must be in 1 .. 2^24");
     OS_REQUIRE(std::isfinite(dbeta), "dbeta must be finite");
     OS_REQUIRE(step >= 0, "step must be >= 0");
     for (uint32_t i = 0; i < population; ++i) OS_REQUIRE(std::isfinite(energies[i]), "energies[%u] not finite", i);
+    activate(ctx);
     cudaStream_t s = ctx->stream;
     DevBuf<double> e, cum, tot, emin, lq;
     DevBuf<int> par;

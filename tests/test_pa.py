@@ -226,3 +226,32 @@ def test_device_slot_range_method_equals_first_exceeding_rule(orc, R, dbeta, sca
         ref, _ = orc.pa_resample(e, dbeta, 31, step)
         assert (par >= 0).all()
         assert np.array_equal(par, ref)
+
+
+def test_population_arguments_are_checked_on_the_host(native):
+    """Parameter checks run before the device is touched (null context here)."""
+    import ctypes as C
+    from tests.test_sa_gpu import chimera_ising
+    L = native.lib()
+    q = native.Csr.from_dense(chimera_ising(1, 0))._c()
+
+    def run(beta, population=16, spb=1, resync=0):
+        b = np.ascontiguousarray(beta, dtype=np.float64)
+        prm = native._PaParams(native._dptr(b), len(b), spb, population, 1, resync)
+        res = native._PaResult()
+        st = L.os_pa_run_sparse(None, C.byref(q), C.byref(prm), C.byref(res))
+        return st, L.os_last_error().decode()
+
+    for args, msg in [(([1.0], 0), "population"), (([1.0], 70000), "population"), (([np.inf],), "finite"),
+                      (([1.0], 16, 0), "sweeps_per_beta"), (([1.0], 16, 1, -2), "resync")]:
+        st, err = run(*args)
+        assert st == native.INVALID_ARG and msg in err, (args, err)
+    st, err = run([0.2, 0.4])
+    assert st == native.INVALID_ARG and "null context" in err
+
+    par = np.zeros(2, dtype=np.int32)
+    lq = C.c_double()
+    e = np.array([0.0, np.nan])
+    st = L.os_pa_resample_replay(None, 2, native._dptr(e), 0.5, 1, 0, par.ctypes.data_as(C.POINTER(C.c_int32)),
+                                 C.byref(lq))
+    assert st == native.INVALID_ARG and "not finite" in L.os_last_error().decode()

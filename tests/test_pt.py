@@ -213,3 +213,40 @@ def test_droplet_512_reaches_tensor_network_ground_state(native, orc, ctx, golde
                                num_rounds=20000, sweeps_per_round=5, resync_every=200, seed=7, ctx=ctx)
     assert res.energy == pytest.approx(orc.energy(f, res.state), rel=1e-9, abs=0)
     assert abs(res.energy - g["tn_ground_qubo"]) < 1e-6, res.energy
+
+
+def test_tempering_arguments_are_checked_on_the_host(native):
+    """The parameter checks run before the device is touched, so they are
+    exercised here without a GPU (a null context): bad parameters are
+    INVALID_ARG with the reason, good ones reach the context check."""
+    import ctypes as C
+    L = native.lib()
+    q = native.Csr.from_dense(chimera_ising(1, 0))._c()
+
+    def run(beta, chains=2, rounds=1, spr=1, resync=0):
+        b = np.ascontiguousarray(beta, dtype=np.float64)
+        prm = native._PtParams(native._dptr(b), len(b), chains, rounds, spr, 1, resync)
+        res = native._PtResult()
+        st = L.os_pt_run_sparse(None, C.byref(q), C.byref(prm), C.byref(res))
+        return st, L.os_last_error().decode()
+
+    for args, msg in [(([1.0, 0.5],), "non-decreasing"), (([np.nan],), "finite"), (([-0.1],), "finite"),
+                      ((np.linspace(0.1, 1, 64), 1025), "65535"), (([1.0], 2, 0), "positive"),
+                      (([1.0], 2, 1, 0), "positive"), (([1.0], 0), "num_chains"), (([1.0], 2, 1, 1, -1), "resync")]:
+        st, err = run(*args)
+        assert st == native.INVALID_ARG and msg in err, (args, err)
+    st, err = run([0.5, 1.0])
+    assert st == native.INVALID_ARG and "null context" in err
+
+    def replay(temps, beta=(0.1, 1.0)):
+        b = np.ascontiguousarray(beta, dtype=np.float64)
+        t = np.ascontiguousarray(temps, dtype=np.int32)
+        e = np.zeros(t.size)
+        st = L.os_pt_exchange_replay(None, t.shape[0], t.shape[1], native._dptr(b), native._dptr(e), 1, 0, 1,
+                                     t.ctypes.data_as(C.POINTER(C.c_int32)), None)
+        return st, L.os_last_error().decode()
+
+    st, err = replay([[0, 0], [0, 1]])
+    assert st == native.INVALID_ARG and "chain 0 is not a permutation" in err
+    st, err = replay([[1, 0], [0, 1]])
+    assert st == native.INVALID_ARG and "null context" in err
