@@ -361,11 +361,11 @@ extern "C" {
 os_status os_sa_plan_create_batched(os_ctx *ctx, int32_t num_instances, const os_qubo_dense *instances,
                                     const os_sa_params *params, os_sa_plan **out) {
   return guard([&] {
-    activate(ctx);
     OS_REQUIRE(out != nullptr, "null output");
     check_schedule(params);
     OS_REQUIRE(params->resync_every >= 0, "resync_every = -1 (no resync) is for dense plans only");
     OS_REQUIRE(num_instances >= 1 && instances, "empty batch");
+    activate(ctx);
     auto *p = new os_sa_plan();
     try {
       p->kind = 2;

@@ -455,10 +455,10 @@ extern "C" {
 os_status os_sa_plan_create_dense(os_ctx *ctx, const os_qubo_dense *qubo, const os_sa_params *params,
                                   os_sa_plan **out) {
   return guard([&] {
-    activate(ctx);
     OS_REQUIRE(out != nullptr, "null output");
     check_schedule(params);
     OS_REQUIRE(qubo != nullptr, "null QUBO");
+    activate(ctx);
     auto *p = new os_sa_plan();
     try {
       p->kind = 0;

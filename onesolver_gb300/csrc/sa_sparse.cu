@@ -1169,13 +1169,13 @@ extern "C" {
 os_status os_sa_plan_create_sparse(os_ctx *ctx, const os_qubo_csr *qubo, const os_sa_params *params,
                                    os_sa_plan **out) {
   return guard([&] {
-    activate(ctx);
     OS_REQUIRE(out != nullptr, "null output");
     check_schedule(params);
     OS_REQUIRE(params->resync_every >= 0, "resync_every = -1 (no resync) is for dense plans only");
     OS_REQUIRE(qubo != nullptr, "null QUBO");
     OS_REQUIRE(params->site_order == OS_SITES_SEQUENTIAL,
                "sparse annealing sweeps all sites per step (site_order must be SEQUENTIAL)");
+    activate(ctx);
     auto *p = new os_sa_plan();
     try {
       p->kind = 1;
