@@ -367,7 +367,6 @@ extern "C" {
 os_status os_exhaustive_plan_create(os_ctx *ctx, const os_qubo_dense *qubo,
                                     const os_exh_params *params, os_exh_plan **out) {
   return guard([&] {
-    activate(ctx);
     OS_REQUIRE(qubo && qubo->f && out, "null argument");
     const int n = qubo->n;
     OS_REQUIRE(n >= 1 && n <= MAX_N, "exhaustive search supports 1..%d variables (got %d)", MAX_N, n);
@@ -408,6 +407,7 @@ os_status os_exhaustive_plan_create(os_ctx *ctx, const os_qubo_dense *qubo,
     if (kind == OS_COEF_INT64)
       OS_REQUIRE(integral && abs_sum < 9.0e15, "coefficients are not int64-exact");
 
+    activate(ctx);
     auto *p = new os_exh_plan();
     try {
       p->ctx = ctx;

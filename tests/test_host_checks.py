@@ -1,4 +1,5 @@
-"""Parameter checks of the annealing entry points, on the CPU.
+"""Parameter checks of the annealing and exhaustive-search entry points, on
+the CPU.
 
 The C ABI validates a call's parameters before it touches the device, so the
 checks run here with a null context: a bad parameter is INVALID_ARG with its
@@ -76,3 +77,33 @@ def test_batched_plan_checks(native):
     prm, b = _params(native, [1.0])
     st = L.os_sa_plan_create_batched(None, 2, arr, C.byref(prm), C.byref(h))
     assert st == native.INVALID_ARG and "null context" in L.os_last_error().decode()
+
+
+def _exh(native, f, **kw):
+    q, keep = native._dense(f)
+    prm = native._ExhParams(kw.get("kind", 0), kw.get("fixed", 0), kw.get("prefix", 0), kw.get("cap", 16),
+                            kw.get("inner", 0), kw.get("variant", 0))
+    h = C.c_void_p()
+    st = native.lib().os_exhaustive_plan_create(None, C.byref(q), C.byref(prm), C.byref(h))
+    return st, native.lib().os_last_error().decode()
+
+
+@pytest.mark.parametrize("f,kw,msg", [
+    (np.zeros((51, 51)), {}, "supports 1..50 variables"),
+    (np.array([[1.0, np.inf], [np.inf, 0.0]]), {}, "coefficient (0,1) is not finite"),
+    (np.eye(6), {"fixed": 6}, "fixed_high_bits must be in [0, n)"),
+    (np.eye(6), {"fixed": 2, "prefix": 4}, "prefix does not fit"),
+    (np.eye(6), {"prefix": 1}, "prefix given without fixed_high_bits"),
+    (np.eye(6), {"inner": 8}, "inner_bits must be 0"),
+    (np.eye(6), {"variant": 9}, "unknown variant 9"),
+    (np.eye(6) * 0.5, {"kind": 1}, "not int32-exact"),
+    (np.eye(6), {"kind": 9}, "unknown coef_kind 9"),
+])
+def test_exhaustive_plan_checks(native, f, kw, msg):
+    st, err = _exh(native, f, **kw)
+    assert st == native.INVALID_ARG and msg in err, err
+
+
+def test_exhaustive_plan_with_good_parameters_reaches_the_context(native):
+    st, err = _exh(native, np.eye(6), fixed=2, prefix=3)
+    assert st == native.INVALID_ARG and "null context" in err
