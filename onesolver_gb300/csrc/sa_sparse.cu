@@ -16,6 +16,12 @@
 // The energy is tracked per sweep and the best state is checked once per
 // sweep. FP64 resyncs recompute the fields from the spins and record the
 // drift of the FP32 fields.
+//
+// The same sweep kernel also serves the two solvers the reference's annealing
+// benchmark names as next (benchmarks/annealing/performance.md:52-59):
+// parallel tempering (each replica at its own inverse temperature, replica
+// exchange between launches) and population annealing (systematic resampling
+// between temperatures, the copy folded into the sweep's state load).
 #include <algorithm>
 #include <cmath>
 #include <cstring>
