@@ -646,7 +646,10 @@ void noalloc_run(const os_qubo_dense *qubo, const os_exh_params &prm, os_exh_res
   for (int i = 0; i < n; ++i)
     for (int j = i; j < n; ++j)
       q[(size_t)i * n + j] = q[(size_t)j * n + i] = (T)qubo->f[(size_t)i * n + j];
-  constexpr int G = G_DEFAULT;
+  // Inner width and instruction variant as os_exhaustive_plan_create
+  // chooses them (the caller's values, else the defaults).
+  const int G = prm.inner_bits ? prm.inner_bits : G_DEFAULT;
+  const int variant = prm.variant ? prm.variant : OS_EXH_VARIANT_DEFAULT;
   GrayParams<T> P{};
   T kf[INNER_MAX];
   if (!small) inner_constants(q, n, G, kf);
@@ -693,7 +696,7 @@ void noalloc_run(const os_qubo_dense *qubo, const os_exh_params &prm, os_exh_res
     ctas = (int)ceil_div_u64(P.nstates, THREADS);
   } else {
     int occ = 0, sms = 0;
-    occ = gray_occupancy_width<T, G>();
+    occ = gray_occupancy<T>(G);
     OS_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
     const unsigned long long want = ceil_div_u64(1ull << P.item_bits, THREADS);
     ctas = (int)std::min<unsigned long long>(want, (unsigned long long)sms * std::max(occ, 1));
@@ -710,7 +713,7 @@ void noalloc_run(const os_qubo_dense *qubo, const os_exh_params &prm, os_exh_res
   if (small) {
     small_kernel<T, false><<<ctas, THREADS, 0, s>>>(P);
   } else {
-    launch_gray_width<T, G>(OS_EXH_VARIANT_ADD_MIN, false, ctas, s, P);
+    launch_gray<T, false>(G, variant, ctas, s, P);
   }
   OS_CUDA(cudaGetLastError());
   gather_kernel<T><<<1, 1024, 0, s>>>(P.cta, ctas, P.cta_states, summary, P.out_states, P.out_cap);
@@ -727,7 +730,7 @@ void noalloc_run(const os_qubo_dense *qubo, const os_exh_params &prm, os_exh_res
     if (small)
       small_kernel<T, true><<<ctas, THREADS, 0, s>>>(P);
     else
-      launch_gray_width<T, G>(OS_EXH_VARIANT_ADD_MIN, true, ctas, s, P);
+      launch_gray<T, true>(G, variant, ctas, s, P);
     OS_CUDA(cudaGetLastError());
     unsigned long long c3[3];
     OS_CUDA(cudaMemcpyAsync(c3, counters + C_OUT_COUNT, sizeof c3, cudaMemcpyDeviceToHost, s));
@@ -768,6 +771,9 @@ extern "C" os_status os_exhaustive_run_noalloc(const os_qubo_dense *qubo, const 
       OS_REQUIRE(prm.prefix < (1ull << prm.fixed_high_bits), "prefix does not fit in fixed_high_bits");
     else
       OS_REQUIRE(prm.prefix == 0, "prefix given without fixed_high_bits");
+    OS_REQUIRE(prm.inner_bits == 0 || prm.inner_bits == 9 || prm.inner_bits == 10,
+               "inner_bits must be 0 (default), 9 or 10");
+    OS_REQUIRE(prm.variant >= 0 && prm.variant <= OS_EXH_VARIANT_FUSED, "unknown variant %d", prm.variant);
     OS_REQUIRE(prm.max_minimisers <= NOALLOC_MAX_OUT,
                "max_minimisers %llu exceeds the no-allocation limit of %llu",
                (unsigned long long)prm.max_minimisers, (unsigned long long)NOALLOC_MAX_OUT);

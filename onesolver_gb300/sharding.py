@@ -73,24 +73,34 @@ def gpu_shard_solver(f: np.ndarray, *, ctx=None, max_minimisers: int = 4096) -> 
     return solve
 
 
+def _gather_on_rank0(obj, world: int, rank: int, group) -> Optional[list]:
+    """torch.distributed.gather_object of `obj` to rank 0 over `group` (None =
+    the default process group, which must be initialised); the list of every
+    rank's object on rank 0, None elsewhere."""
+    import torch.distributed as dist
+    if not dist.is_available() or not dist.is_initialized():
+        raise ValueError("world > 1 needs an initialised torch.distributed process group")
+    gathered = [None] * world if rank == 0 else None
+    dist.gather_object(obj, gathered, dst=0, group=group)
+    return gathered
+
+
 def exhaustive_sharded(f: np.ndarray, solve_shard: Callable[[int, int], ShardRecord], *, world: int = 1,
-                       rank: int = 0, process_group=None, shards_per_rank: int = 4,
+                       rank: int = 0, group=None, shards_per_rank: int = 4,
                        max_minimisers: Optional[int] = None) -> Optional[ShardRecord]:
     """Enumerate this rank's shards with `solve_shard(k, prefix)` (e.g.
     `gpu_shard_solver(f)`), then gather the records on rank 0 and merge them.
-    Returns the merged record on rank 0 and None elsewhere; with world == 1
-    no process group is needed."""
+    Returns the merged record on rank 0 and None elsewhere. With world > 1
+    the records travel over `group` (a torch.distributed ProcessGroup; None =
+    the default group); with world == 1 no process group is needed."""
     n = f.shape[0]
     k = shard_bits(n, world, shards_per_rank)
     mine = [solve_shard(k, p) for p in shard_prefixes(world, rank, k)]
     local = merge_records(mine) if mine else ShardRecord(math.inf, np.zeros(0, np.uint64), 0, 0)
     if world == 1:
         return merge_records([local], max_minimisers)
-    if process_group is None:
-        raise ValueError("world > 1 needs a process group (torch.distributed)")
-    gathered = [None] * world if rank == 0 else None
     payload = (local.energy, local.states.tolist(), local.count, local.states_enumerated)
-    process_group.gather_object(payload, gathered, dst=0)
+    gathered = _gather_on_rank0(payload, world, rank, group)
     if rank != 0:
         return None
     return merge_records([ShardRecord(e, np.asarray(s, dtype=np.uint64), c, m) for e, s, c, m in gathered],
@@ -125,16 +135,14 @@ class ReplicaBest:
 
 
 def best_over_ranks(energy: float, state: np.ndarray, *, world: int = 1, rank: int = 0,
-                    process_group=None) -> Optional[ReplicaBest]:
-    """Gather every rank's best (energy, state) on rank 0 and return the first
-    minimum in rank order there (None on the other ranks)."""
+                    group=None) -> Optional[ReplicaBest]:
+    """Gather every rank's best (energy, state) on rank 0 over `group` (a
+    torch.distributed ProcessGroup; None = the default group) and return the
+    first minimum in rank order there (None on the other ranks)."""
     state = np.asarray(state, dtype=np.uint8)
     if world == 1:
         return ReplicaBest(float(energy), state, 0)
-    if process_group is None:
-        raise ValueError("world > 1 needs a process group (torch.distributed)")
-    gathered = [None] * world if rank == 0 else None
-    process_group.gather_object((float(energy), state.tobytes()), gathered, dst=0)
+    gathered = _gather_on_rank0((float(energy), state.tobytes()), world, rank, group)
     if rank != 0:
         return None
     best = 0
@@ -146,9 +154,9 @@ def best_over_ranks(energy: float, state: np.ndarray, *, world: int = 1, rank: i
 
 
 def solve_replicas(solve: Callable[[int], tuple], seed: int, *, world: int = 1, rank: int = 0,
-                   process_group=None) -> Optional[ReplicaBest]:
+                   group=None) -> Optional[ReplicaBest]:
     """Run `solve(seed)` -> (energy, state) with this rank's replica seed
     (e.g. `lambda s: (r := temper_sparse(csr, beta, seed=s)).energy, r.state`)
     and merge on rank 0."""
     e, state = solve(replica_seed(seed, rank))
-    return best_over_ranks(e, state, world=world, rank=rank, process_group=process_group)
+    return best_over_ranks(e, state, world=world, rank=rank, group=group)

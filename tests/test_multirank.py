@@ -51,7 +51,9 @@ def _worker(rank, world, port, n, seed, out_dir):
     dist.init_process_group("gloo", rank=rank, world_size=world)
     try:
         f = _int_qubo(n, seed)
-        rec = sharding.exhaustive_sharded(f, oracle_shard_solver(f), world=world, rank=rank, process_group=dist)
+        # An explicit ProcessGroup object (not the torch.distributed module).
+        group = dist.new_group(list(range(world)))
+        rec = sharding.exhaustive_sharded(f, oracle_shard_solver(f), world=world, rank=rank, group=group)
         # bench.py's max-over-ranks timing reduction
         import bench
         t = bench.max_over_ranks(dist, float(rank + 1) * 1.5)
@@ -141,7 +143,7 @@ def _replica_worker(rank, world, port, out_dir):
             return float(energies[k]), np.asarray(states[k], dtype=np.uint8)
 
         e, s = solve(sharding.replica_seed(77, rank))
-        best = sharding.solve_replicas(solve, 77, world=world, rank=rank, process_group=dist)
+        best = sharding.solve_replicas(solve, 77, world=world, rank=rank)
         np.savez(os.path.join(out_dir, f"rep{rank}.npz"), e=e, s=s,
                  best_e=np.nan if best is None else best.energy,
                  best_s=np.zeros(0, np.uint8) if best is None else best.state,

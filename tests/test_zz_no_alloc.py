@@ -22,9 +22,9 @@ from tests.qubo_text import random_int_qubo
 pytestmark = pytest.mark.gpu
 
 
-def noalloc(native, f, cap, fixed_high_bits=0, prefix=0, coef_kind=0):
+def noalloc(native, f, cap, fixed_high_bits=0, prefix=0, coef_kind=0, inner_bits=0, variant=0):
     q, keep = native._dense(f)
-    prm = native._ExhParams(coef_kind, fixed_high_bits, prefix, cap)
+    prm = native._ExhParams(coef_kind, fixed_high_bits, prefix, cap, inner_bits, variant)
     states = np.zeros(max(cap, 1), dtype=np.uint64)
     res = native._ExhResult()
     res.states = states.ctypes.data_as(C.POINTER(C.c_uint64))
@@ -54,7 +54,34 @@ def test_noalloc_matches_run_on_consecutive_calls(native):
     assert (ra1.energy, ra1.state, ra1.count) == (ra2.energy, ra2.state, ra2.count)
     same(native, ctx, a, 4096, fixed_high_bits=4, prefix=9)
     same(native, ctx, random_int_qubo(18, 1, -10 ** 8, 10 ** 8), 64)  # int64 enumeration
+    # The caller's inner width and instruction variant are honoured.
+    for g, v in ((9, 1), (10, 1), (9, 2)):
+        same(native, ctx, a, 4096, inner_bits=g, variant=v)
     ctx.close()
+
+
+def test_noalloc_leaves_device_memory_unchanged(native):
+    """The calls take no device memory: the device's free memory is the same
+    before and after a series of calls (the first calls, which load the
+    kernels and look up the array's address, come before the measurement)."""
+    torch = pytest.importorskip("torch")
+    a = random_int_qubo(30, 7)
+    b = random_int_qubo(12, 3, -1, 1)
+    z = np.zeros((20, 20))
+
+    def calls():
+        for f, cap in ((a, 4096), (b, 4096), (z, 1000)):
+            st, _, _ = noalloc(native, f, cap)
+            assert st in (native.OK, native.OVERFLOW_MINIMISERS), native.lib().os_last_error()
+
+    calls()
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    for _ in range(3):
+        calls()
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0
 
 
 def test_noalloc_collection_pass(native):
@@ -80,3 +107,9 @@ def test_noalloc_rejects_out_of_range_requests(native):
     st, _, _ = noalloc(native, np.random.default_rng(0).normal(size=(10, 10)), 16)
     assert st == native.INVALID_ARG
     assert b"integer coefficients only" in native.lib().os_last_error()
+    st, _, _ = noalloc(native, f, 16, inner_bits=8)
+    assert st == native.INVALID_ARG
+    assert b"inner_bits" in native.lib().os_last_error()
+    st, _, _ = noalloc(native, f, 16, variant=3)
+    assert st == native.INVALID_ARG
+    assert b"variant" in native.lib().os_last_error()
