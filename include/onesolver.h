@@ -214,10 +214,13 @@ void os_exhaustive_plan_destroy(os_exh_plan *plan);
  *   - Integer coefficients only (int32 or int64 enumeration); non-integer
  *     instances return OS_INVALID_ARG (use os_exhaustive_run).
  *   - n <= 50 and max_minimisers <= OS_NOALLOC_MAX_MINIMISERS; larger
- *     requests return OS_INVALID_ARG.
+ *     requests return OS_INVALID_ARG. inner_bits and variant are checked and
+ *     honoured as os_exhaustive_run does.
  *   - The first call on a device looks up the array's device address
- *     (cudaGetSymbolAddress); make that first call before any stream
- *     capture.
+ *     (cudaGetSymbolAddress), so it belongs before any stream capture on
+ *     that device.
+ *   - Every call copies the answer back into the caller's host buffers and
+ *     waits on `stream` for that before it returns.
  *   - Every call reuses the same array, so calls whose work overlaps on the
  *     GPU (other host threads, other streams) race; serialise them. */
 #define OS_NOALLOC_SCRATCH_BYTES (3u << 20)
@@ -313,16 +316,17 @@ os_status os_sa_run_batched(os_ctx *ctx, int32_t num_instances,
                             const os_qubo_dense *instances,
                             const os_sa_params *params, os_sa_result *results);
 
-/* Deterministic verification mode. Runs the reference's Metropolis rule
- * (annealing.hpp:87-125) on the GPU with caller-given randoms in place of
- * oneMKL's philox4x32x10: init[t*n+i] replaces bit(), site[t*S+a] replaces
- * bit_index() and u[t*S+a] replaces uniform() for attempt a of trajectory t,
- * S = num_iter * sweeps_per_beta. One (site, u) pair is consumed per attempt
- * whether or not u is needed. Energies are tracked from FP64 local fields;
- * for integer-valued coefficients they equal the reference's per-attempt
- * full recomputation exactly, so the spin trajectories are bit-identical.
- * Outputs per trajectory: best state and energy, final state and energy,
- * accepted-flip count (any output pointer may be NULL). */
+/* The reference's kernel body (annealing.hpp:87-125) with caller-given
+ * randoms, one GPU thread per trajectory with FP64 local fields: init[t*n+i]
+ * replaces bit(), site[t*S+a] replaces bit_index() and u[t*S+a] replaces
+ * uniform() for attempt a of trajectory t, S = num_iter * sweeps_per_beta.
+ * One (site, u) pair is consumed per attempt whether or not u is needed.
+ * For integer-valued coefficients the energies equal the reference's
+ * per-attempt full recomputation exactly. This is a separate scalar kernel,
+ * not the sweep kernels of os_sa_run; those are verified by the plans'
+ * replay mode (os_sa_plan_set_replay). Outputs per trajectory: best state
+ * and energy, final state and energy, accepted-flip count (any output
+ * pointer may be NULL). */
 os_status os_sa_verify(os_ctx *ctx, const os_qubo_dense *qubo,
                        const double *beta, int32_t num_iter,
                        int32_t sweeps_per_beta, uint32_t num_tries,
@@ -362,6 +366,50 @@ int32_t os_sa_plan_launches(const os_sa_plan *plan);
  * CUDA events recorded on the context's stream around each of them. */
 os_status os_sa_plan_kernel_ms(os_sa_plan *plan, float *ms);
 void os_sa_plan_destroy(os_sa_plan *plan);
+
+/* Replay (deterministic verification) mode of a dense, sparse or batched
+ * plan. The reference draws its randoms from oneMKL's philox4x32x10
+ * (annealing.hpp:87,91-93,101,108), which cannot be reproduced; in replay
+ * mode the plan's next executes take them from the caller instead and run
+ * everything else unchanged: the same sweep kernels (their replay
+ * instantiation), visit order, field updates, energy and best-state
+ * bookkeeping and FP64 resyncs. Replaces the randoms of annealing.hpp:
+ *   init       initial spins, 0 / nonzero per variable (bit(), :91-93):
+ *              [T][n]; batched plans: instance after instance, [T][n_k] each
+ *   threshold  attempt at site k in step s of trajectory t accepts when
+ *              dE < threshold (uniform() and the test of :106-108 in
+ *              threshold form: -beta ln u for the reference rule,
+ *              -ln(u) / beta for the physical rule). Sequential sweeps:
+ *              [T][steps][n] indexed by site (batched: per instance, as init);
+ *              random sites: [T][steps]
+ *   site       random sites only: [T][steps], the site of each attempt
+ *              (bit_index(), :101); NULL for sequential sweeps
+ * steps = num_iter * sweeps_per_beta. NULL `replay` returns the plan to
+ * Philox draws. */
+typedef struct os_sa_replay {
+  const char *init;
+  const float *threshold;
+  const int32_t *site;
+} os_sa_replay;
+os_status os_sa_plan_set_replay(os_sa_plan *plan, const os_sa_replay *replay);
+
+/* Per-trajectory state after the last execute, for checking a replay (any
+ * pointer may be NULL): final and best spins (bytes, [T][n]; batched:
+ * instance after instance), the tracked energy of the final state and the
+ * best tracked energy (the kernels' running energies, FP32 for dense and
+ * batched plans, FP64 sums of FP32 differences for sparse plans, reset by
+ * every FP64 resync), and the accepted flips. Best states are checked after
+ * every accepted flip by the dense and batched kernels (annealing.hpp:
+ * 115-121) and at the end of every sweep by the sparse kernel. */
+os_status os_sa_plan_trajectories(os_sa_plan *plan, char *final_states, char *best_states,
+                                  double *energies, double *best_energies, uint64_t *accepted);
+
+/* The site order of one sequential sweep of the plan (n entries; batched:
+ * each instance's n_k entries, instance after instance). Dense kernels visit
+ * slot by slot (slot s = the 32 sites 128 (s / 4) + 4 l + s mod 4, lanes l
+ * in order); the sparse kernel visits the colour classes in order, every
+ * class in the listed order. OS_INVALID_ARG for random-site plans. */
+os_status os_sa_plan_sweep_order(const os_sa_plan *plan, int32_t *order);
 
 /* ------------------------------------------------------------------------ */
 /* Parallel tempering (replica exchange)                                    */

@@ -174,6 +174,10 @@ SIGNATURES = {
     "os_sa_plan_result_batched": (C.c_int, [_P, C.POINTER(_SaResult)]),
     "os_sa_plan_tuned_warps": (C.c_int32, [_P]),
     "os_sa_plan_kernel_ms": (C.c_int, [_P, C.POINTER(C.c_float)]),
+    "os_sa_plan_set_replay": (C.c_int, [_P, _P]),
+    "os_sa_plan_trajectories": (C.c_int, [_P, C.c_char_p, C.c_char_p, C.POINTER(C.c_double),
+                                          C.POINTER(C.c_double), C.POINTER(C.c_uint64)]),
+    "os_sa_plan_sweep_order": (C.c_int, [_P, C.POINTER(C.c_int32)]),
     "os_pt_run_sparse": (C.c_int, [_P, C.POINTER(_QuboCsr), C.POINTER(_PtParams), C.POINTER(_PtResult)]),
     "os_pt_exchange_replay": (C.c_int, [_P, C.c_uint32, C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_double),
                                         C.c_uint64, C.c_int32, C.c_int32, C.POINTER(C.c_int32),
@@ -617,7 +621,81 @@ def anneal_sparse(csr: Csr, beta: Sequence[float], *, num_tries: int = 100, swee
     return _finish_sa(res, keep, csr.n, num_tries)
 
 
-class AnnealPlan:
+class _SaReplay(C.Structure):
+    _fields_ = [("init", C.c_char_p), ("threshold", C.POINTER(C.c_float)), ("site", C.POINTER(C.c_int32))]
+
+
+@dataclass
+class Trajectories:
+    """Per-trajectory state of a plan after its last execute (one instance)."""
+    final_states: np.ndarray    # uint8[T, n]
+    best_states: np.ndarray     # uint8[T, n]
+    energies: np.ndarray        # float64[T], tracked energy of the final state
+    best_energies: np.ndarray   # float64[T], best tracked energy
+    accepted: np.ndarray        # uint64[T], accepted flips
+
+
+class _PlanReplay:
+    """Replay (verification) mode shared by the dense, sparse and batched plans:
+    caller-given initial spins and per-attempt thresholds (random sites: and
+    sites) in place of the Philox draws, the rest of the plan unchanged."""
+
+    def _sizes(self) -> list:
+        raise NotImplementedError
+
+    def set_replay(self, init, threshold, site=None) -> None:
+        """init: [T, n] 0/1 (batched: one array per instance); threshold:
+        [T, steps, n] for sequential sweeps (batched: one per instance) or
+        [T, steps] for random sites, float32 (the attempt accepts when
+        dE < threshold); site: [T, steps] for random sites."""
+        if isinstance(init, np.ndarray):
+            init, threshold = [init], [threshold]
+        self._rp_init = np.ascontiguousarray(np.concatenate([np.asarray(a, np.uint8).reshape(-1) for a in init]))
+        self._rp_thr = np.ascontiguousarray(
+            np.concatenate([np.asarray(a, np.float32).reshape(-1) for a in threshold]))
+        self._rp_site = None if site is None else np.ascontiguousarray(site, dtype=np.int32)
+        rp = _SaReplay(self._rp_init.ctypes.data_as(C.c_char_p),
+                       self._rp_thr.ctypes.data_as(C.POINTER(C.c_float)),
+                       None if self._rp_site is None else self._rp_site.ctypes.data_as(C.POINTER(C.c_int32)))
+        _check(lib().os_sa_plan_set_replay(self._h, C.byref(rp)))
+
+    def clear_replay(self) -> None:
+        _check(lib().os_sa_plan_set_replay(self._h, None))
+
+    def trajectories(self):
+        """Trajectories of the last execute (a list, one per instance, for batched plans)."""
+        sizes = self._sizes()
+        T = self.T
+        nv = T * sum(sizes)
+        G = T * len(sizes)
+        fs = C.create_string_buffer(max(nv, 1))
+        bs = C.create_string_buffer(max(nv, 1))
+        e = np.zeros(G)
+        eb = np.zeros(G)
+        acc = np.zeros(G, dtype=np.uint64)
+        _check(lib().os_sa_plan_trajectories(self._h, C.cast(fs, C.c_char_p), C.cast(bs, C.c_char_p), _dptr(e),
+                                             _dptr(eb), acc.ctypes.data_as(C.POINTER(C.c_uint64))))
+        f_all = np.frombuffer(fs.raw[:nv], np.uint8)
+        b_all = np.frombuffer(bs.raw[:nv], np.uint8)
+        out, off = [], 0
+        for k, n in enumerate(sizes):
+            sl = slice(off, off + T * n)
+            g = slice(k * T, (k + 1) * T)
+            out.append(Trajectories(f_all[sl].reshape(T, n).copy(), b_all[sl].reshape(T, n).copy(), e[g].copy(),
+                                    eb[g].copy(), acc[g].copy()))
+            off += T * n
+        return out if len(sizes) > 1 or isinstance(self, BatchedAnnealPlan) else out[0]
+
+    def sweep_order(self):
+        """Site order of one sequential sweep (a list per instance for batched plans)."""
+        sizes = self._sizes()
+        order = np.zeros(sum(sizes), dtype=np.int32)
+        _check(lib().os_sa_plan_sweep_order(self._h, order.ctypes.data_as(C.POINTER(C.c_int32))))
+        parts = np.split(order, np.cumsum(sizes)[:-1])
+        return parts if isinstance(self, BatchedAnnealPlan) else parts[0]
+
+
+class AnnealPlan(_PlanReplay):
     """Device-resident anneal (dense or sparse): create / execute / result."""
 
     def __init__(self, qubo, beta: Sequence[float], *, num_tries: int = 100, sweeps_per_beta: int = 1,
@@ -661,6 +739,9 @@ class AnnealPlan:
         res, keep = _sa_result(self.n, self.T, traj_states)
         _check(lib().os_sa_plan_result(self._h, C.byref(res)))
         return _finish_sa(res, keep, self.n, self.T)
+
+    def _sizes(self) -> list:
+        return [self.n]
 
     def close(self) -> None:
         if self._h:
@@ -834,7 +915,7 @@ def anneal_batched(instances, beta: Sequence[float], *, num_tries: int = 256, sw
     return [_finish_sa(res[k], keeps[k], fs[k].shape[0], num_tries) for k in range(len(fs))]
 
 
-class BatchedAnnealPlan:
+class BatchedAnnealPlan(_PlanReplay):
     """Device-resident batched anneal: create (autotunes) / execute (graph replay) / result."""
 
     def __init__(self, instances, beta: Sequence[float], *, num_tries: int = 256, sweeps_per_beta: int = 1,
@@ -870,6 +951,9 @@ class BatchedAnnealPlan:
         res, keeps = _batch_results(self._fs, self.T, traj_states)
         _check(lib().os_sa_plan_result_batched(self._h, res))
         return [_finish_sa(res[k], keeps[k], self._fs[k].shape[0], self.T) for k in range(len(self._fs))]
+
+    def _sizes(self) -> list:
+        return [f.shape[0] for f in self._fs]
 
     def close(self) -> None:
         if self._h:

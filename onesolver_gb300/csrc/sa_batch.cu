@@ -24,6 +24,7 @@
 #include "sa_common.cuh"
 #include "sa_kernels.cuh"
 #include "sa_plan.cuh"
+#include "sa_replay.cuh"
 
 namespace os {
 namespace sa {
@@ -119,6 +120,9 @@ BatchArgs batch_args(os_sa_plan *p, BatchState &B, int W, int s0, int s1) {
   a.ebest = p->ebest.get();
   a.accepted = p->accepted.get();
   a.status = p->status.get();
+  a.thr = p->replay ? p->rp_thr.get() : nullptr;
+  a.state_off = B.state_off.get();
+  a.nsteps = p->steps;
   return a;
 }
 
@@ -136,6 +140,8 @@ BatchResyncArgs resync_args(os_sa_plan *p, BatchState &B, int init) {
   r.e = p->e.get();
   r.ebest = p->ebest.get();
   r.drift_bits = p->drift.get();
+  r.init_bits = p->replay ? p->rp_init.get() : nullptr;
+  r.state_off = B.state_off.get();
   return r;
 }
 
@@ -310,7 +316,10 @@ void enqueue_batched(os_sa_plan *p, BatchState &B, cudaStream_t s) {
     // External records: inside the captured graph they become event-record
     // nodes that the host can wait on after a replay.
     OS_CUDA(cudaEventRecordWithFlags(p->event(2 * chunk), s, cudaEventRecordExternal));
-    OS_BATCH_DISPATCH(p->slot_cls, launch_batch_tile, a, B.grid, B.smem, s);
+    if (p->replay)
+      batch_tile_replay(a, p->slot_cls, B.grid, B.smem, s);
+    else
+      OS_BATCH_DISPATCH(p->slot_cls, launch_batch_tile, a, B.grid, B.smem, s);
     OS_CUDA(cudaGetLastError());
     OS_CUDA(cudaEventRecordWithFlags(p->event(2 * chunk + 1), s, cudaEventRecordExternal));
     OS_BATCH_DISPATCH(p->slot_cls, launch_batch_resync, r, s);
@@ -348,6 +357,17 @@ void execute_batched(os_sa_plan *p) {
 void release_batch(os_sa_plan *p) {
   delete p->batch;
   p->batch = nullptr;
+}
+
+std::vector<int> batch_sizes(const os_sa_plan *p) { return p->batch->n; }
+
+void batch_replay_changed(os_sa_plan *p) {
+  BatchState &B = *p->batch;
+  if (B.graph) {
+    OS_CUDA(cudaGraphExecDestroy(B.graph));
+    B.graph = nullptr;
+  }
+  if (p->replay) batch_replay_smem(p->slot_cls, B.smem);
 }
 
 }  // namespace sa

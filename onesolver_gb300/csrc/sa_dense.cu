@@ -1,5 +1,6 @@
-// sa_dense.cu -- dense simulated annealing: the verification kernel, the
-// device-resident plan and the os_sa_run / os_sa_verify entry points.
+// sa_dense.cu -- dense simulated annealing: the device-resident plan, the
+// os_sa_run entry point and os_sa_verify (the reference's one-thread-per-
+// trajectory loop with caller-given randoms).
 //
 // Replaces sa::anneal (include/simulated_annealing/annealing.hpp:55-140).
 // One anneal is: draw the initial spins and compute the FP64 fields; run the
@@ -18,6 +19,7 @@
 #include "sa_kernels.cuh"
 #include "sa_init.cuh"
 #include "sa_plan.cuh"
+#include "sa_replay.cuh"
 
 namespace os {
 namespace sa {
@@ -120,9 +122,6 @@ template <int SLOTS> void launch_resync(const ResyncArgs &a, int warps, cudaStre
     case 64: fn<64>(__VA_ARGS__); break;                                \
     default: throw_error(OS_INVALID_ARG, "unsupported slot count %d", cls); \
   }
-
-// Largest padded row length whose two 16-row tiles fit in shared memory.
-constexpr int TILE_MAX_LD = 1792;
 
 void dense_sweeps(const DenseArgs &a, int slot_cls, int warps, bool sequential, cudaStream_t s) {
   if (sequential && a.ld <= TILE_MAX_LD) {
@@ -279,6 +278,7 @@ InitArgs dense_init_args(os_sa_plan *p) {
   a.xbest = p->xbest.get();
   a.e = p->e.get();
   a.ebest = p->ebest.get();
+  a.init_bits = p->replay ? p->rp_init.get() : nullptr;
   return a;
 }
 
@@ -304,6 +304,9 @@ DenseArgs dense_args(os_sa_plan *p) {
   a.ebest = p->ebest.get();
   a.accepted = p->accepted.get();
   a.status = p->status.get();
+  a.thr = p->replay ? p->rp_thr.get() : nullptr;
+  a.rsite = p->replay && !p->sequential ? p->rp_site.get() : nullptr;
+  a.nsteps = p->steps;
   return a;
 }
 
@@ -365,7 +368,10 @@ void execute_dense(os_sa_plan *p) {
     a.step_begin = s0;
     a.step_end = std::min(p->steps, s0 + chunk);
     OS_CUDA(cudaEventRecord(p->event(2 * p->sweep_ev_used), s));
-    dense_sweeps(a, p->slot_cls, p->warps, p->sequential, s);
+    if (p->replay)
+      dense_sweeps_replay(a, p->slot_cls, p->warps, p->sequential, s);
+    else
+      dense_sweeps(a, p->slot_cls, p->warps, p->sequential, s);
     OS_CUDA(cudaEventRecord(p->event(2 * p->sweep_ev_used + 1), s));
     ++p->sweep_ev_used;
     ++p->launches;

@@ -87,6 +87,7 @@ __global__ void init_spins_kernel(const InitArgs a, int t0, int count, __nv_bflo
     if (site < a.n) {
       const uint32_t v = (s & 3) == 0 ? r.x : (s & 3) == 1 ? r.y : (s & 3) == 2 ? r.z : r.w;
       bit = a.init_prob ? (u01_open(v) < a.init_prob[site]) : (v >> 31) != 0;
+      if (a.init_bits) bit = a.init_bits[(size_t)t * a.n + site] != 0;
     }
     if (bit) xl |= 1ull << s;
     row[site] = bit ? one : zero;

@@ -22,6 +22,7 @@ struct InitArgs {
   float *h;                // fields [T][nslots/2][32] FP32 pairs
   unsigned long long *x, *xbest;
   float *e, *ebest;
+  const uint8_t *init_bits; // optional initial spins [T][n] (replay mode)
 };
 
 // Split the plan's FP64 couplings into the three BF16 terms of the product

@@ -35,6 +35,16 @@
 // u ~ U(0,1) from Philox, the reference rule exp((E - E') / beta) > u is
 // dE < -beta ln u and the physical rule exp(-beta dE) > u is
 // dE < -ln(u) / beta.
+//
+// Replay (verification) mode: every sweep kernel has a REPLAY instantiation
+// that reads the threshold of each attempt (and, for random sites, the site)
+// from caller-given arrays instead of drawing it from Philox, and the
+// initialisation kernels can take caller-given initial spins. Everything else
+// (visit order, ballot rounds, field updates, energy and best-state
+// bookkeeping, tiles, resyncs) is the production code path, so a replay on
+// integer coefficients, where the FP32 fields and energies are exact, must
+// reproduce a CPU transcription of the reference's Metropolis loop
+// (annealing.hpp:97-123) in the kernel's site order bit for bit.
 #ifndef ONESOLVER_SA_KERNELS_CUH_
 #define ONESOLVER_SA_KERNELS_CUH_
 
@@ -75,6 +85,12 @@ struct DenseArgs {
   float *ebest;            // [traj]
   unsigned long long *accepted;  // [traj]
   int *status;             // set to 1 when a bounded wait ran out
+  // Replay mode only (REPLAY kernels): thresholds and sites of trajectory 0
+  // of this launch; sequential sweeps read thr[(t * nsteps + step) * n +
+  // site], random sites thr[t * nsteps + step] and rsite[t * nsteps + step].
+  const float *thr;
+  const int *rsite;
+  int nsteps;              // steps of the whole run (row length of thr, rsite)
 };
 
 __device__ __forceinline__ float select4(const Philox4 &r, int j) {
@@ -154,7 +170,7 @@ template <int SLOTS> struct Fields {
 // Sequential-order sweeps over [step_begin, step_end), one trajectory per
 // warp, rows read from global memory (used when two staged row tiles do not
 // fit in shared memory).
-template <int SLOTS>
+template <int SLOTS, bool REPLAY = false>
 __global__ void __launch_bounds__(128) sa_dense_seq_kernel(const __grid_constant__ DenseArgs a) {
   const int lane = threadIdx.x & 31;
   const int t = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
@@ -176,11 +192,16 @@ __global__ void __launch_bounds__(128) sa_dense_seq_kernel(const __grid_constant
 #pragma unroll
     for (int s = 0; s < SLOTS; ++s) {
       if (s >= nslots) break;
-      if ((s & 3) == 0)
-        r = philox4x32_10((uint32_t)((s >> 2) * 32 + lane), (uint32_t)step, tg, c3, a.seed_lo, a.seed_hi);
-      const float theta = threshold(select4(r, s & 3), b, a.acceptance);
       const int site = slot_site(s, lane);
       const bool valid = site < a.n;
+      float theta;
+      if constexpr (REPLAY) {
+        theta = valid ? a.thr[((size_t)t * a.nsteps + step) * a.n + site] : 0.f;
+      } else {
+        if ((s & 3) == 0)
+          r = philox4x32_10((uint32_t)((s >> 2) * 32 + lane), (uint32_t)step, tg, c3, a.seed_lo, a.seed_hi);
+        theta = threshold(select4(r, s & 3), b, a.acceptance);
+      }
       const float d = a.diag[site];
       const unsigned xs0 = __ballot_sync(FULL, (xl >> s) & 1ull);  // spins at the start of the slot
       int p = 0;
@@ -217,7 +238,7 @@ __global__ void __launch_bounds__(128) sa_dense_seq_kernel(const __grid_constant
 
 // Random-order steps (the reference's one random site per step,
 // annealing.hpp:97-101) for one trajectory per warp.
-template <int SLOTS>
+template <int SLOTS, bool REPLAY = false>
 __global__ void __launch_bounds__(128) sa_dense_rand_kernel(const __grid_constant__ DenseArgs a) {
   const int lane = threadIdx.x & 31;
   const int t = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
@@ -234,14 +255,21 @@ __global__ void __launch_bounds__(128) sa_dense_rand_kernel(const __grid_constan
   const uint32_t c3 = (a.instance & 0x0FFFFFFFu) | kStreamSite;
   Philox4 r{0, 0, 0, 0};
   for (int step = a.step_begin; step < a.step_end; ++step) {
-    const float b = (float)a.beta[step / a.spb];
-    if ((step & 1) == 0 || step == a.step_begin)
-      r = philox4x32_10((uint32_t)(step >> 1), 0u, tg, c3, a.seed_lo, a.seed_hi);
-    const bool second = step & 1;
-    const uint32_t wk = second ? r.z : r.x;
-    const uint32_t wu = second ? r.w : r.y;
-    const int k = (int)__umulhi(wk, (uint32_t)a.n);
-    const float theta = threshold(u01_open(wu), b, a.acceptance);
+    int k;
+    float theta;
+    if constexpr (REPLAY) {
+      k = a.rsite[(size_t)t * a.nsteps + step];
+      theta = a.thr[(size_t)t * a.nsteps + step];
+    } else {
+      const float b = (float)a.beta[step / a.spb];
+      if ((step & 1) == 0 || step == a.step_begin)
+        r = philox4x32_10((uint32_t)(step >> 1), 0u, tg, c3, a.seed_lo, a.seed_hi);
+      const bool second = step & 1;
+      const uint32_t wk = second ? r.z : r.x;
+      const uint32_t wu = second ? r.w : r.y;
+      k = (int)__umulhi(wk, (uint32_t)a.n);
+      theta = threshold(u01_open(wu), b, a.acceptance);
+    }
     const int slot = site_slot(k), owner = site_lane(k);
     float hv = 0.f;
 #pragma unroll
@@ -286,13 +314,15 @@ __global__ void __launch_bounds__(128) sa_dense_rand_kernel(const __grid_constan
 // current sweep.
 constexpr int TILE_ROWS = 16;
 constexpr uint32_t TILE_WAIT_LIMIT = 1u << 26;
+// Largest padded row length whose two 16-row tiles fit in shared memory.
+constexpr int TILE_MAX_LD = 1792;
 
 // One item: the W trajectories of `a` (pointers already at the item's first
 // trajectory, warp w runs trajectory w), steps [step_begin, step_end).
 // `tiles` holds two buffers of TILE_ROWS x ld floats, `bar` their mbarriers,
 // `parity` their phase bits (kept by the caller across items). Returns false
 // when a bounded wait ran out (uniformly for the whole CTA).
-template <int SLOTS, bool ALL>
+template <int SLOTS, bool ALL, bool REPLAY>
 __device__ __forceinline__ bool tile_item_impl(const DenseArgs &a, float *tiles, uint64_t *bar,
                                                uint32_t (&parity)[2]) {
   const int lane = threadIdx.x & 31;
@@ -338,11 +368,16 @@ __device__ __forceinline__ bool tile_item_impl(const DenseArgs &a, float *tiles,
 #pragma unroll
     for (int s = 0; s < SLOTS; ++s) {
       if (s >= nslots) break;
-      if ((s & 3) == 0)
-        r = philox4x32_10((uint32_t)((s >> 2) * 32 + lane), (uint32_t)step, tg, c3, a.seed_lo, a.seed_hi);
-      const float theta = threshold(select4(r, s & 3), b, a.acceptance);
       const int site = slot_site(s, lane);
       const bool valid = site < a.n;
+      float theta;
+      if constexpr (REPLAY) {
+        theta = (active && valid) ? a.thr[((size_t)t * a.nsteps + step) * a.n + site] : 0.f;
+      } else {
+        if ((s & 3) == 0)
+          r = philox4x32_10((uint32_t)((s >> 2) * 32 + lane), (uint32_t)step, tg, c3, a.seed_lo, a.seed_hi);
+        theta = threshold(select4(r, s & 3), b, a.acceptance);
+      }
       const float d = a.diag[site];
 #pragma unroll
       for (int half = 0; half < 2; ++half) {
@@ -405,10 +440,10 @@ __device__ __forceinline__ bool tile_item_impl(const DenseArgs &a, float *tiles,
 // An instance whose slot count fills the kernel's class (nslots == SLOTS)
 // takes the variant without per-group padding tests (8% faster at
 // n = 1024); the others keep the tests.
-template <int SLOTS>
+template <int SLOTS, bool REPLAY = false>
 __device__ __forceinline__ bool tile_item(const DenseArgs &a, float *tiles, uint64_t *bar, uint32_t (&parity)[2]) {
-  return a.nslots == SLOTS ? tile_item_impl<SLOTS, true>(a, tiles, bar, parity)
-                           : tile_item_impl<SLOTS, false>(a, tiles, bar, parity);
+  return a.nslots == SLOTS ? tile_item_impl<SLOTS, true, REPLAY>(a, tiles, bar, parity)
+                           : tile_item_impl<SLOTS, false, REPLAY>(a, tiles, bar, parity);
 }
 
 __device__ __forceinline__ void init_tile_barriers(uint64_t *bar) {
@@ -421,7 +456,7 @@ __device__ __forceinline__ void init_tile_barriers(uint64_t *bar) {
 }
 
 // One CTA per block of W trajectories of one instance.
-template <int SLOTS>
+template <int SLOTS, bool REPLAY = false>
 __global__ void __launch_bounds__(512) sa_dense_tile_kernel(const __grid_constant__ DenseArgs a) {
   extern __shared__ __align__(128) unsigned char tile_smem[];
   __shared__ __align__(8) uint64_t bar[2];
@@ -437,8 +472,9 @@ __global__ void __launch_bounds__(512) sa_dense_tile_kernel(const __grid_constan
   it.e = a.e + first;
   it.ebest = a.ebest + first;
   it.accepted = a.accepted + first;
+  if constexpr (REPLAY) it.thr = a.thr + first * a.nsteps * a.n;
   uint32_t parity[2] = {0u, 0u};
-  tile_item<SLOTS>(it, reinterpret_cast<float *>(tile_smem), bar, parity);
+  tile_item<SLOTS, REPLAY>(it, reinterpret_cast<float *>(tile_smem), bar, parity);
 }
 
 // Many instances in one persistent launch: items are (instance, block of W
@@ -468,9 +504,15 @@ struct BatchArgs {
   float *e, *ebest;
   unsigned long long *accepted;
   int *status;
+  // Replay mode only: thresholds of all trajectories of all instances,
+  // instance after instance, [T][nsteps][n_k] each; trajectory g's block
+  // starts at nsteps * state_off[g].
+  const float *thr;
+  const long long *state_off;
+  int nsteps;
 };
 
-template <int SLOTS>
+template <int SLOTS, bool REPLAY = false>
 __global__ void __launch_bounds__(512) sa_batch_tile_kernel(const __grid_constant__ BatchArgs B) {
   extern __shared__ __align__(128) unsigned char tile_smem[];
   __shared__ __align__(8) uint64_t bar[2];
@@ -509,7 +551,11 @@ __global__ void __launch_bounds__(512) sa_batch_tile_kernel(const __grid_constan
     a.ebest = B.ebest + g0;
     a.accepted = B.accepted + g0;
     a.status = B.status;
-    if (!tile_item<SLOTS>(a, reinterpret_cast<float *>(tile_smem), bar, parity)) break;
+    if constexpr (REPLAY) {
+      a.thr = B.thr + (long long)B.nsteps * B.state_off[g0];
+      a.nsteps = B.nsteps;
+    }
+    if (!tile_item<SLOTS, REPLAY>(a, reinterpret_cast<float *>(tile_smem), bar, parity)) break;
   }
 }
 
@@ -527,6 +573,7 @@ struct ResyncArgs {
   float *e;
   float *ebest;
   unsigned long long *drift_bits;  // max |h32 - h64| as ordered FP64 bits
+  const uint8_t *init_bits;        // optional initial spins [traj][n] (replay mode)
 };
 
 // FP64 field resync (and initialisation) of trajectory t of `a`:
@@ -550,6 +597,7 @@ __device__ __forceinline__ void resync_traj(const ResyncArgs &a, int t) {
       if (site >= a.n) continue;
       const uint32_t w = (s & 3) == 0 ? r.x : (s & 3) == 1 ? r.y : (s & 3) == 2 ? r.z : r.w;
       bool bit = a.init_prob ? (u01_open(w) < a.init_prob[site]) : (w >> 31) != 0;
+      if (a.init_bits) bit = a.init_bits[(size_t)t * a.n + site] != 0;
       if (bit) xl |= 1ull << s;
     }
   } else {
@@ -621,6 +669,10 @@ struct BatchResyncArgs {
   unsigned long long *x, *xbest;
   float *e, *ebest;
   unsigned long long *drift_bits;
+  // Replay mode only: initial spins of all trajectories, instance after
+  // instance ([T][n_k] each); trajectory g's row starts at state_off[g].
+  const uint8_t *init_bits;
+  const long long *state_off;
 };
 
 template <int SLOTS>
@@ -649,6 +701,7 @@ __global__ void __launch_bounds__(128) sa_batch_resync_kernel(const __grid_const
   a.e = B.e + in.traj_base;
   a.ebest = B.ebest + in.traj_base;
   a.drift_bits = B.drift_bits;
+  a.init_bits = B.init_bits ? B.init_bits + B.state_off[in.traj_base] : nullptr;
   resync_traj<SLOTS>(a, t);
 }
 

@@ -72,6 +72,15 @@ struct os_sa_plan {
   os::DevBuf<double> se, sebest;            // energies [T]
   std::vector<int> host_row_ptr, host_col;
   std::vector<double> host_val, host_diag;
+  std::vector<int> host_color_sites;        // sweep order: the sites colour by colour
+
+  // Replay (verification) mode, os_sa_plan_set_replay: caller-given initial
+  // spins and per-attempt thresholds (and sites, random order) take the
+  // place of the Philox draws in the same kernels.
+  bool replay = false;
+  os::DevBuf<uint8_t> rp_init;
+  os::DevBuf<float> rp_thr;
+  os::DevBuf<int> rp_site;
 };
 
 void os_sa_plan_common(os_sa_plan *p, os_ctx *ctx, const os_sa_params *prm, int n);
@@ -82,6 +91,11 @@ void execute_dense(os_sa_plan *p);
 void execute_sparse(os_sa_plan *p);
 void execute_batched(os_sa_plan *p);
 void release_batch(os_sa_plan *p);
+// Batched plans: variables of each instance, and a change of replay mode
+// (drops the captured execute graph so the next execute captures the
+// kernels of the new mode).
+std::vector<int> batch_sizes(const os_sa_plan *p);
+void batch_replay_changed(os_sa_plan *p);
 }  // namespace sa
 }  // namespace os
 

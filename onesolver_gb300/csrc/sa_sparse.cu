@@ -66,6 +66,10 @@ struct SparseArgs {
   const double *e_in, *ebest_in;
   const int *anc_in;
   int *anc;
+  // Replay mode only (REPLAY kernel): the threshold of every attempt,
+  // thr[(t * nsteps + step) * n + site], in place of the Philox draws.
+  const float *thr;
+  int nsteps;
 };
 
 enum SweepMode : int { kAnneal = 0, kTemper = 1, kPopulation = 2 };
@@ -99,7 +103,7 @@ __device__ __forceinline__ void apply_updates(const uint32_t *__restrict__ list,
 // beta[temp[t]] for the whole launch. kPopulation: annealing whose
 // trajectories start from their resampled parents (population annealing);
 // the copy rides on the launch's own state load.
-template <int MODE>
+template <int MODE, bool REPLAY = false>
 __global__ void __launch_bounds__(256, 8) sa_sparse_kernel(const __grid_constant__ SparseArgs a) {
   extern __shared__ unsigned char smem[];
   const int R = a.traj_per_cta;
@@ -165,8 +169,9 @@ __global__ void __launch_bounds__(256, 8) sa_sparse_kernel(const __grid_constant
       // sites with the same Philox counters as a per-thread loop would.
       for (int wbase = tid - lane; wbase < cnt; wbase += 4 * tpt) {
         const int mybase = wbase + lane;
-        const Philox4 r = philox4x32_10((uint32_t)(c0 + mybase), (uint32_t)step, (uint32_t)t, c3, a.seed_lo,
-                                        a.seed_hi);
+        Philox4 r{0, 0, 0, 0};
+        if constexpr (!REPLAY)
+          r = philox4x32_10((uint32_t)(c0 + mybase), (uint32_t)step, (uint32_t)t, c3, a.seed_lo, a.seed_hi);
         int listed = 0;  // warp-uniform
 #pragma unroll
         for (int m = 0; m < 4; ++m) {
@@ -177,9 +182,14 @@ __global__ void __launch_bounds__(256, 8) sa_sparse_kernel(const __grid_constant
           bool neg = false;
           if (valid) {
             k = a.color_sites[c0 + idx];
-            const uint32_t w = m == 0 ? r.x : m == 1 ? r.y : m == 2 ? r.z : r.w;
-            const float l = __logf(u01_open(w));
-            const float theta = a.acceptance == OS_ACCEPT_REFERENCE ? -b * l : -l * inv_b;
+            float theta;
+            if constexpr (REPLAY) {
+              theta = a.thr[((size_t)t * a.nsteps + step) * n + k];
+            } else {
+              const uint32_t w = m == 0 ? r.x : m == 1 ? r.y : m == 2 ? r.z : r.w;
+              const float l = __logf(u01_open(w));
+              theta = a.acceptance == OS_ACCEPT_REFERENCE ? -b * l : -l * inv_b;
+            }
             const float loc = a.diag[k] + h[k];
             const bool xk = x[k];
             const float dE = xk ? -loc : loc;
@@ -268,9 +278,11 @@ struct SparseResyncArgs {
   double *e;
   double *ebest;
   unsigned long long *drift_bits;
+  const uint8_t *init_bits;   // optional initial spins [T][n] (replay mode)
 };
 
-// Initial spins (one Philox call per four sites of a trajectory).
+// Initial spins (one Philox call per four sites of a trajectory, or the
+// caller's spins in replay mode).
 __global__ void sa_sparse_init_kernel(const __grid_constant__ SparseResyncArgs a) {
   const int t = blockIdx.y;
   const int g = blockIdx.x * blockDim.x + threadIdx.x;  // group of 4 sites
@@ -282,7 +294,8 @@ __global__ void sa_sparse_init_kernel(const __grid_constant__ SparseResyncArgs a
   for (int m = 0; m < 4; ++m) {
     const int k = 4 * g + m;
     if (k >= a.n) break;
-    const bool bit = a.init_prob ? (u01_open(w[m]) < a.init_prob[k]) : (w[m] >> 31) != 0;
+    bool bit = a.init_prob ? (u01_open(w[m]) < a.init_prob[k]) : (w[m] >> 31) != 0;
+    if (a.init_bits) bit = a.init_bits[(size_t)t * a.n + k] != 0;
     a.x[(size_t)t * a.n + k] = bit;
   }
 }
@@ -444,6 +457,7 @@ void plan_create_sparse(os_sa_plan *p, const os_qubo_csr *q) {
   csites.resize(n);
   std::vector<int> fill(cptr.begin(), cptr.end() - 1);
   for (int v = 0; v < n; ++v) csites[fill[color[v]]++] = v;
+  p->host_color_sites = csites;
   std::vector<float> v32(vl.begin(), vl.end()), d32(dg.begin(), dg.end());
 
   p->n = n;
@@ -504,7 +518,8 @@ void plan_create_sparse(os_sa_plan *p, const os_qubo_csr *q) {
   OS_REQUIRE(per <= 200 * 1024, "sparse instance too large for shared memory (%d variables)", n);
   p->traj_per_cta = R;
   p->warps = tpt * R / 32;
-  for (auto fn : {sa_sparse_kernel<kAnneal>, sa_sparse_kernel<kTemper>, sa_sparse_kernel<kPopulation>})
+  for (auto fn : {sa_sparse_kernel<kAnneal>, sa_sparse_kernel<kTemper>, sa_sparse_kernel<kPopulation>,
+                  sa_sparse_kernel<kAnneal, true>})
     OS_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)std::max<size_t>(per * R, 48 * 1024)));
 }
@@ -535,6 +550,7 @@ static SparseResyncArgs start_sparse(os_sa_plan *p) {
   r.e = p->se.get();
   r.ebest = p->sebest.get();
   r.drift_bits = p->drift.get();
+  r.init_bits = p->replay ? p->rp_init.get() : nullptr;
   dim3 ig((unsigned)ceil_div_u64((n + 3) / 4, 128), T);
   sa_sparse_init_kernel<<<ig, 128, 0, s>>>(r);
   OS_CUDA(cudaGetLastError());
@@ -572,6 +588,8 @@ static SparseArgs sweep_args(os_sa_plan *p, const SparseResyncArgs &r) {
   a.ebest = p->sebest.get();
   a.accepted = p->accepted.get();
   a.temp = nullptr;
+  a.thr = p->replay ? p->rp_thr.get() : nullptr;
+  a.nsteps = p->steps;
   return a;
 }
 
@@ -602,7 +620,10 @@ void execute_sparse(os_sa_plan *p) {
     a.step_begin = s0;
     a.step_end = std::min(p->steps, s0 + p->chunk);
     OS_CUDA(cudaEventRecord(p->event(2 * p->sweep_ev_used), s));
-    sa_sparse_kernel<kAnneal><<<grid, threads, smem, s>>>(a);
+    if (p->replay)
+      sa_sparse_kernel<kAnneal, true><<<grid, threads, smem, s>>>(a);
+    else
+      sa_sparse_kernel<kAnneal><<<grid, threads, smem, s>>>(a);
     OS_CUDA(cudaGetLastError());
     OS_CUDA(cudaEventRecord(p->event(2 * p->sweep_ev_used + 1), s));
     ++p->sweep_ev_used;

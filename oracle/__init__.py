@@ -58,12 +58,19 @@ def lib() -> C.CDLL:
         L.orc_exhaustive.restype = None
         L.orc_exhaustive_all.argtypes = [_D, C.c_int, C.c_uint64, C.c_uint64, C.c_int, _D, _U64, C.c_uint64]
         L.orc_exhaustive_all.restype = C.c_uint64
+        L.orc_exhaustive_int_all.argtypes = [_D, C.c_int, C.c_uint64, C.c_uint64, C.c_int,
+                                             C.POINTER(C.c_int64), _U64, C.c_uint64]
+        L.orc_exhaustive_int_all.restype = C.c_int64
         L.orc_anneal_verify.argtypes = [_D, C.c_int, _D, C.c_int, C.c_int, C.c_int, C.c_char_p, _I, _D, C.c_int,
                                         C.c_char_p, _D, C.c_char_p, _D, C.POINTER(C.c_int64)]
         L.orc_anneal_verify.restype = None
         L.orc_anneal_free.argtypes = [_D, C.c_int, _D, C.c_int, C.c_int, C.c_int, C.c_uint64, C.c_int, C.c_int,
                                       C.c_int, C.c_char_p, _D]
         L.orc_anneal_free.restype = C.c_int64
+        L.orc_sa_replay.argtypes = [_D, C.c_int, _D, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _I,
+                                    C.c_char_p, _I, _D, C.c_int, C.c_int, C.c_char_p, C.c_char_p, _D, _D,
+                                    C.POINTER(C.c_int64)]
+        L.orc_sa_replay.restype = None
         L.orc_argmin.argtypes = [_D, C.c_int]
         L.orc_argmin.restype = C.c_int
         L.orc_philox4x32_10.argtypes = [C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]
@@ -150,6 +157,23 @@ def exhaustive_all(f: np.ndarray, begin: int = 0, end: Optional[int] = None, thr
     return e.value, int(count), np.sort(states[: min(count, cap)])
 
 
+def exhaustive_int_all(f: np.ndarray, begin: int = 0, end: Optional[int] = None, threads: int = 0,
+                       cap: int = 1 << 16):
+    """(energy, count, ascending minimisers) of an integer-coefficient QUBO, every
+    state's energy evaluated on its own from per-row byte tables (exact in int64)."""
+    f = np.ascontiguousarray(f, dtype=np.float64)
+    n = f.shape[0]
+    end = (1 << n) if end is None else end
+    threads = threads or (os.cpu_count() or 1)
+    e = C.c_int64()
+    states = np.zeros(max(cap, 1), dtype=np.uint64)
+    count = lib().orc_exhaustive_int_all(_d(f), n, begin, end, threads, C.byref(e),
+                                         states.ctypes.data_as(_U64), cap)
+    if count < 0:
+        raise ValueError("exhaustive_int_all needs integer coefficients (|q| < 2^40) and 1 <= n <= 63")
+    return float(e.value), int(count), states[: min(count, cap)].copy()
+
+
 def anneal_verify(f, beta, init, site, u, sweeps_per_beta=1, acceptance=0):
     f = np.ascontiguousarray(f, dtype=np.float64)
     n = f.shape[0]
@@ -181,6 +205,36 @@ def anneal_free(f, beta, num_tries, sweeps_per_beta=1, seed=1, acceptance=0, sit
     att = lib().orc_anneal_free(_d(f), n, _d(beta), len(beta), num_tries, sweeps_per_beta, seed, acceptance,
                                 site_order, threads, C.cast(bs, C.c_char_p), _d(be))
     return np.frombuffer(bs.raw[: num_tries * n], np.uint8).reshape(num_tries, n).copy(), be, int(att)
+
+
+def sa_replay(f, beta, init, u, *, sweeps_per_beta=1, acceptance=0, mode=1, order=None, site=None,
+              full_energy=False, threads=0):
+    """The reference's Metropolis loop (annealing.hpp:97-123) on given randoms in a
+    given site order (orc_sa_replay): mode 0 random sites (site [T, S], u [T, S]),
+    1 sequential sweeps in `order` with the best state checked after every
+    attempt, 2 the same with the best state checked at the end of every sweep
+    (u [T, S, n] by site). Returns (final_states, best_states, final_energies,
+    best_energies, accepted)."""
+    f = np.ascontiguousarray(f, dtype=np.float64)
+    n = f.shape[0]
+    beta = np.ascontiguousarray(beta, dtype=np.float64)
+    init = np.ascontiguousarray(init, dtype=np.uint8)
+    T = init.shape[0]
+    u = np.ascontiguousarray(u, dtype=np.float64)
+    order_a = np.ascontiguousarray(np.arange(n) if order is None else order, dtype=np.int32)
+    site_a = np.ascontiguousarray(np.zeros(1) if site is None else site, dtype=np.int32)
+    threads = threads or min(16, os.cpu_count() or 1)
+    fs = C.create_string_buffer(T * n)
+    bs = C.create_string_buffer(T * n)
+    fe = np.zeros(T)
+    be = np.zeros(T)
+    ac = np.zeros(T, dtype=np.int64)
+    lib().orc_sa_replay(_d(f), n, _d(beta), len(beta), sweeps_per_beta, T, acceptance, mode,
+                        order_a.ctypes.data_as(_I), init.ctypes.data_as(C.c_char_p), site_a.ctypes.data_as(_I),
+                        _d(u), 1 if full_energy else 0, threads, C.cast(fs, C.c_char_p), C.cast(bs, C.c_char_p),
+                        _d(fe), _d(be), ac.ctypes.data_as(C.POINTER(C.c_int64)))
+    return (np.frombuffer(fs.raw[: T * n], np.uint8).reshape(T, n).copy(),
+            np.frombuffer(bs.raw[: T * n], np.uint8).reshape(T, n).copy(), fe, be, ac)
 
 
 def philox(ctr, key) -> list[int]:

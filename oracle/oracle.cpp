@@ -262,6 +262,84 @@ uint64_t orc_exhaustive_all(const double *flat, int n, uint64_t begin,
   return count;
 }
 
+// All exact minimisers over [begin, end) of an integer-coefficient QUBO, for
+// state spaces too large for the O(n^2)-per-state loop of orc_exhaustive_all
+// (2^36 states at n = 36). Every state's energy is still evaluated on its
+// own, as the reference's work-item loop does (exhaustive.hpp:110-129):
+//   E(s) = sum_{i set} ( Q_ii + sum_{j > i, j set} Q_ij ),
+// with the inner sum over j read a byte of the state at a time from per-row
+// tables U_i[b][v] = sum of Q_ij over the set bits j of byte value v in byte
+// b (j > i only). With integer coefficients every partial sum is an integer
+// far below 2^53, so the int64 value equals the reference's FP64 sum in any
+// order. Returns the total number of minimisers (up to cap of them written
+// to states in ascending order) and the minimum in *e_out; returns -1 when a
+// coefficient on or above the diagonal is not an integer of magnitude below
+// 2^40. Threads take blocks of 2^16 states from a shared counter.
+int64_t orc_exhaustive_int_all(const double *flat, int n, uint64_t begin, uint64_t end, int nthreads,
+                               int64_t *e_out, uint64_t *states, uint64_t cap) {
+  if (n < 1 || n > 63 || end <= begin) return -1;
+  if (nthreads < 1) nthreads = 1;
+  const int nb = (n + 7) / 8;
+  std::vector<int64_t> diag(n);
+  std::vector<int64_t> tab((size_t)n * nb * 256, 0);
+  for (int i = 0; i < n; ++i) {
+    for (int j = i; j < n; ++j) {
+      const double v = flat[(size_t)i * n + j];
+      if (!(std::fabs(v) < 0x1.0p40) || v != std::floor(v)) return -1;
+    }
+    diag[i] = (int64_t)flat[(size_t)i * n + i];
+    for (int b = 0; b < nb; ++b)
+      for (int v = 0; v < 256; ++v) {
+        int64_t s = 0;
+        for (int k = 0; k < 8; ++k) {
+          const int j = 8 * b + k;
+          if (j > i && j < n && ((v >> k) & 1)) s += (int64_t)flat[(size_t)i * n + j];
+        }
+        tab[((size_t)i * nb + b) * 256 + v] = s;
+      }
+  }
+  const uint64_t block = 1ull << 16;
+  std::atomic<uint64_t> next{begin};
+  std::vector<int64_t> emin(nthreads, std::numeric_limits<int64_t>::max());
+  std::vector<std::vector<uint64_t>> found(nthreads);
+  auto worker = [&](int t) {
+    int64_t em = std::numeric_limits<int64_t>::max();
+    std::vector<uint64_t> &f = found[t];
+    for (;;) {
+      const uint64_t lo = next.fetch_add(block);
+      if (lo >= end) break;
+      const uint64_t hi = std::min(end, lo + block);
+      for (uint64_t s = lo; s < hi; ++s) {
+        int64_t e = 0;
+        for (uint64_t m = s; m; m &= m - 1) {
+          const int i = __builtin_ctzll(m);
+          const int64_t *row = &tab[(size_t)i * nb * 256];
+          int64_t r = diag[i];
+          for (int b = i >> 3; b < nb; ++b) r += row[b * 256 + ((s >> (8 * b)) & 255)];
+          e += r;
+        }
+        if (e < em) {
+          em = e;
+          f.clear();
+        }
+        if (e == em) f.push_back(s);
+      }
+    }
+    emin[t] = em;
+  };
+  std::vector<std::thread> pool;
+  for (int t = 0; t < nthreads; ++t) pool.emplace_back(worker, t);
+  for (auto &th : pool) th.join();
+  const int64_t best = *std::min_element(emin.begin(), emin.end());
+  std::vector<uint64_t> all;
+  for (int t = 0; t < nthreads; ++t)
+    if (emin[t] == best) all.insert(all.end(), found[t].begin(), found[t].end());
+  std::sort(all.begin(), all.end());
+  for (uint64_t k = 0; k < all.size() && k < cap; ++k) states[k] = all[k];
+  *e_out = best;
+  return (int64_t)all.size();
+}
+
 // Deterministic verification transcription of sa::anneal's kernel body,
 // include/simulated_annealing/annealing.hpp:87-125, for one trajectory per
 // row of the precomputed arrays.
@@ -330,6 +408,118 @@ void orc_anneal_verify(const double *flat, int n, const double *beta,
     if (final_energies) final_energies[t] = current_energy;
     if (accept_count) accept_count[t] = acc;
   }
+}
+
+// Replay transcription of sa::anneal's kernel body
+// (include/simulated_annealing/annealing.hpp:97-123) in a given site order,
+// for checking the GPU sweep kernels' replay mode bit for bit.
+//
+// Trajectory t starts from init[t*n ..] (:91-93). Step a = iter *
+// sweeps_per_beta + sweep runs at beta[iter] (:97-99) and is
+//   mode 0: one attempt at site[t*S + a] (:101), u = u[t*S + a];
+//   mode 1, 2: one attempt at every site in order[0 .. n) (a sequential
+//           sweep), u = u[(t*S + a)*n + k] for site k;
+// with S = num_iter * sweeps_per_beta. An attempt flips the site, takes the
+// energy of the flipped state, keeps the flip when new_energy <
+// current_energy or the acceptance test passes, else flips back (:102-113):
+// acceptance 0 is exp((current_energy - new_energy) / beta) > u, 1 is
+// exp(-beta * (new_energy - current_energy)) > u. The best state and energy
+// are updated when current_energy < best_energy (:115-121) after every
+// attempt (modes 0 and 1), or after the last attempt of every sweep only
+// (mode 2: the sparse kernel's bookkeeping).
+//
+// full_energy 1 evaluates every new_energy from scratch with the
+// reference's energy function (:104); 0 keeps FP64 local fields
+// h_k = sum_{j != k} F[k][j] x_j, new_energy = current_energy +
+// (1 - 2 x_k)(F[k][k] + h_k), which equals it exactly when the
+// coefficients are integers (every partial sum an integer below 2^53) and
+// costs O(n) per accepted flip instead of O(n^2) per attempt.
+//
+// Outputs per trajectory: final and best states, final and best energies,
+// accepted flips. Trajectories are spread over nthreads host threads.
+void orc_sa_replay(const double *flat, int n, const double *beta, int num_iter, int sweeps_per_beta,
+                   int num_tries, int acceptance, int mode, const int *order, const char *init,
+                   const int *site, const double *u, int full_energy, int nthreads, char *final_states,
+                   char *best_states, double *final_energies, double *best_energies,
+                   int64_t *accept_count) {
+  if (nthreads < 1) nthreads = 1;
+  const int64_t S = (int64_t)num_iter * sweeps_per_beta;
+  std::atomic<int> next{0};
+  auto worker = [&]() {
+    std::vector<char> cur(n), best(n);
+    std::vector<double> h(n);
+    for (;;) {
+      const int t = next.fetch_add(1);
+      if (t >= num_tries) break;
+      for (int i = 0; i < n; ++i) cur[i] = init[(size_t)t * n + i] ? 1 : 0;
+      best = cur;
+      for (int k = 0; k < n; ++k) {
+        double acc = 0.0;
+        for (int j = 0; j < n; ++j)
+          if (j != k && cur[j]) acc += j < k ? flat[(size_t)j * n + k] : flat[(size_t)k * n + j];
+        h[k] = acc;
+      }
+      double best_energy = energy_ref(flat, cur.data(), n);
+      double current_energy = best_energy;
+      int64_t acc = 0;
+      auto attempt = [&](int k, double b, double uu) {
+        cur[k] = 1 - cur[k];
+        double new_energy;
+        if (full_energy) {
+          new_energy = energy_ref(flat, cur.data(), n);
+        } else {
+          const double loc = flat[(size_t)k * n + k] + h[k];
+          new_energy = current_energy + (cur[k] ? loc : -loc);
+        }
+        bool keep = new_energy < current_energy;
+        if (!keep)
+          keep = acceptance == 0 ? std::exp((current_energy - new_energy) / b) > uu
+                                 : std::exp(-b * (new_energy - current_energy)) > uu;
+        if (keep) {
+          current_energy = new_energy;
+          ++acc;
+          if (!full_energy) {
+            const double sgn = cur[k] ? 1.0 : -1.0;
+            for (int j = 0; j < n; ++j)
+              if (j != k) h[j] += sgn * (j < k ? flat[(size_t)j * n + k] : flat[(size_t)k * n + j]);
+          }
+        } else {
+          cur[k] = 1 - cur[k];
+        }
+      };
+      for (int iter = 0; iter < num_iter; iter++) {
+        const double b = beta[iter];
+        for (int sweep = 0; sweep < sweeps_per_beta; sweep++) {
+          const int64_t a = (int64_t)iter * sweeps_per_beta + sweep;
+          if (mode == 0) {
+            attempt(site[(size_t)t * S + a], b, u[(size_t)t * S + a]);
+          } else {
+            const double *ua = u + ((size_t)t * S + a) * n;
+            for (int m = 0; m < n; ++m) {
+              const int k = order[m];
+              attempt(k, b, ua[k]);
+              if (mode == 1 && current_energy < best_energy) {
+                best_energy = current_energy;
+                best = cur;
+              }
+            }
+          }
+          if (mode != 1 && current_energy < best_energy) {
+            best_energy = current_energy;
+            best = cur;
+          }
+        }
+      }
+      std::memcpy(final_states + (size_t)t * n, cur.data(), n);
+      std::memcpy(best_states + (size_t)t * n, best.data(), n);
+      final_energies[t] = current_energy;
+      best_energies[t] = best_energy;
+      accept_count[t] = acc;
+    }
+  };
+  std::vector<std::thread> pool;
+  for (int i = 0; i < nthreads; ++i) pool.emplace_back(worker);
+  for (auto &th : pool) th.join();
 }
 
 // Free-running CPU anneal with the reference algorithm (full FP64 energy
