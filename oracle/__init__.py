@@ -71,6 +71,9 @@ def lib() -> C.CDLL:
                                     C.c_char_p, _I, _D, C.c_int, C.c_int, C.c_char_p, C.c_char_p, _D, _D,
                                     C.POINTER(C.c_int64)]
         L.orc_sa_replay.restype = None
+        L.orc_anneal_free_fields.argtypes = [_D, C.c_int, _D, C.c_int, C.c_int, C.c_int, C.c_uint64, C.c_int,
+                                             C.c_int, _I, C.c_int, C.c_int, C.c_char_p, _D]
+        L.orc_anneal_free_fields.restype = C.c_int64
         L.orc_argmin.argtypes = [_D, C.c_int]
         L.orc_argmin.restype = C.c_int
         L.orc_philox4x32_10.argtypes = [C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]
@@ -204,6 +207,23 @@ def anneal_free(f, beta, num_tries, sweeps_per_beta=1, seed=1, acceptance=0, sit
     be = np.zeros(num_tries)
     att = lib().orc_anneal_free(_d(f), n, _d(beta), len(beta), num_tries, sweeps_per_beta, seed, acceptance,
                                 site_order, threads, C.cast(bs, C.c_char_p), _d(be))
+    return np.frombuffer(bs.raw[: num_tries * n], np.uint8).reshape(num_tries, n).copy(), be, int(att)
+
+
+def anneal_free_fields(f, beta, num_tries, sweeps_per_beta=1, seed=1, acceptance=0, site_order=0, order=None,
+                       best_at_sweep_end=False, threads=0):
+    """The free-running reference chain with FP64 local fields and a given
+    sweep order (orc_anneal_free_fields): (best states, best energies, attempts)."""
+    f = np.ascontiguousarray(f, dtype=np.float64)
+    n = f.shape[0]
+    beta = np.ascontiguousarray(beta, dtype=np.float64)
+    threads = threads or (os.cpu_count() or 1)
+    order_a = None if order is None else np.ascontiguousarray(order, dtype=np.int32)
+    bs = C.create_string_buffer(num_tries * n)
+    be = np.zeros(num_tries)
+    att = lib().orc_anneal_free_fields(_d(f), n, _d(beta), len(beta), sweeps_per_beta, num_tries, seed, acceptance,
+                                       site_order, None if order_a is None else order_a.ctypes.data_as(_I),
+                                       1 if best_at_sweep_end else 0, threads, C.cast(bs, C.c_char_p), _d(be))
     return np.frombuffer(bs.raw[: num_tries * n], np.uint8).reshape(num_tries, n).copy(), be, int(att)
 
 

@@ -587,6 +587,104 @@ int64_t orc_anneal_free(const double *flat, int n, const double *beta,
   return attempts.load();
 }
 
+// The free-running anneal of orc_anneal_free (same host RNG stream, same
+// draws in the same order: the initial bits, then per attempt the site in
+// random order and the uniform only when new_energy >= current_energy, the
+// short-circuit of annealing.hpp:106-108), with two changes for large
+// instances:
+//   * energies are kept in FP64 local fields over the nonzero couplings,
+//     new_energy = current_energy + (1 - 2 x_k)(F[k][k] + h_k), which equals
+//     the reference's per-attempt recomputation (:104) exactly for integer
+//     coefficients and to rounding otherwise, at O(degree) per accepted flip;
+//   * a sequential sweep visits order[0 .. n) (NULL: 0 .. n-1), so the chain
+//     can be the one a GPU kernel runs in its own site order.
+// best_at_sweep_end = 1 checks the best state at the end of every step only
+// (the sparse kernel's bookkeeping) instead of after every attempt
+// (:115-121). With order = NULL and best_at_sweep_end = 0 the output on an
+// integer instance is orc_anneal_free's, bit for bit. Returns the attempts.
+int64_t orc_anneal_free_fields(const double *flat, int n, const double *beta, int num_iter, int sweeps_per_beta,
+                               int num_tries, uint64_t seed, int acceptance, int site_order, const int *order,
+                               int best_at_sweep_end, int nthreads, char *best_states, double *best_energies) {
+  if (nthreads < 1) nthreads = 1;
+  // Nonzero couplings of every site (upper triangle mirrored).
+  std::vector<int> ptr(n + 1, 0), nb;
+  std::vector<double> cv;
+  for (int k = 0; k < n; ++k) {
+    for (int j = 0; j < n; ++j) {
+      if (j == k) continue;
+      const double c = j < k ? flat[(size_t)j * n + k] : flat[(size_t)k * n + j];
+      if (c != 0.0) {
+        nb.push_back(j);
+        cv.push_back(c);
+      }
+    }
+    ptr[k + 1] = (int)nb.size();
+  }
+  std::atomic<int> next{0};
+  std::atomic<int64_t> attempts{0};
+  auto worker = [&]() {
+    std::vector<char> cur(n), best(n);
+    std::vector<double> h(n);
+    for (;;) {
+      const int t = next.fetch_add(1);
+      if (t >= num_tries) break;
+      HostRng rng(seed * 0x9E3779B97F4A7C15ull + (uint64_t)t * 0xD1B54A32D192ED03ull + 1);
+      for (int i = 0; i < n; ++i) cur[i] = (char)(rng.next() >> 63);
+      best = cur;
+      for (int k = 0; k < n; ++k) {
+        double acc = 0.0;
+        for (int e = ptr[k]; e < ptr[k + 1]; ++e)
+          if (cur[nb[e]]) acc += cv[e];
+        h[k] = acc;
+      }
+      double best_energy = energy_ref(flat, cur.data(), n);
+      double current_energy = best_energy;
+      int64_t local = 0;
+      for (int iter = 0; iter < num_iter; iter++) {
+        const double b = beta[iter];
+        for (int sweep = 0; sweep < sweeps_per_beta; sweep++) {
+          const int inner = site_order == 1 ? n : 1;
+          for (int s = 0; s < inner; ++s) {
+            const int k = site_order == 1 ? (order ? order[s] : s) : rng.below(n);
+            const double loc = flat[(size_t)k * n + k] + h[k];
+            const double new_energy = current_energy + (cur[k] ? -loc : loc);
+            bool accept;
+            if (new_energy < current_energy) {
+              accept = true;
+            } else {
+              const double uu = rng.uniform();
+              accept = acceptance == 0 ? std::exp((current_energy - new_energy) / b) > uu
+                                       : std::exp(-b * (new_energy - current_energy)) > uu;
+            }
+            if (accept) {
+              cur[k] = 1 - cur[k];
+              current_energy = new_energy;
+              const double sgn = cur[k] ? 1.0 : -1.0;
+              for (int e = ptr[k]; e < ptr[k + 1]; ++e) h[nb[e]] += sgn * cv[e];
+            }
+            if (!best_at_sweep_end && current_energy < best_energy) {
+              best_energy = current_energy;
+              best = cur;
+            }
+            ++local;
+          }
+          if (best_at_sweep_end && current_energy < best_energy) {
+            best_energy = current_energy;
+            best = cur;
+          }
+        }
+      }
+      std::memcpy(best_states + (size_t)t * n, best.data(), n);
+      best_energies[t] = best_energy;
+      attempts += local;
+    }
+  };
+  std::vector<std::thread> pool;
+  for (int i = 0; i < nthreads; ++i) pool.emplace_back(worker);
+  for (auto &th : pool) th.join();
+  return attempts.load();
+}
+
 // Host-side argmin over trajectories, annealing.hpp:134-139 (first minimum).
 int orc_argmin(const double *e, int m) {
   return (int)(std::min_element(e, e + m) - e);

@@ -88,3 +88,31 @@ def test_thresholds_agree_with_the_exp_rule():
         for de in range(-40, 41):
             ref = (de < 0) | (np.exp(-de / bs) > u if acceptance == 0 else np.exp(-bs * de) > u)
             assert np.array_equal(de < thr, ref)
+
+
+@pytest.mark.parametrize("site_order,acceptance", [(0, 0), (0, 1), (1, 0), (1, 1)])
+def test_local_field_chain_equals_the_reference_chain(orc, site_order, acceptance):
+    """orc_anneal_free_fields draws the same randoms in the same order as the
+    reference-algorithm anneal (full FP64 energy per attempt): on an integer
+    instance the two give the same best states and energies, bit for bit."""
+    n, T = 22, 12
+    f = random_int_qubo(n, 31, -4, 4)
+    beta = np.geomspace(8.0, 0.5, 15) if acceptance == 0 else np.geomspace(0.05, 1.5, 15)
+    a = orc.anneal_free(f, beta, T, 3, seed=17, acceptance=acceptance, site_order=site_order)
+    b = orc.anneal_free_fields(f, beta, T, 3, seed=17, acceptance=acceptance, site_order=site_order)
+    assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1]) and a[2] == b[2]
+
+
+def test_local_field_chain_sweep_order_and_bookkeeping(orc):
+    """A given sweep order and sweep-end bookkeeping: best energies are the
+    energies of the best states, never below the per-attempt bookkeeping's."""
+    n, T = 40, 16
+    f = random_int_qubo(n, 8, -3, 3)
+    beta = np.geomspace(0.05, 2.0, 20)
+    order = np.random.default_rng(0).permutation(n)
+    a = orc.anneal_free_fields(f, beta, T, 1, seed=3, acceptance=1, site_order=1, order=order)
+    b = orc.anneal_free_fields(f, beta, T, 1, seed=3, acceptance=1, site_order=1, order=order,
+                               best_at_sweep_end=True)
+    assert np.array_equal(orc.energy_batch(f, a[0]), a[1])
+    assert np.array_equal(orc.energy_batch(f, b[0]), b[1])
+    assert np.all(b[1] >= a[1])

@@ -264,10 +264,17 @@ def test_sparse_energy_distribution_matches_oracle(native, orc, ctx):
     f = chimera_ising(2, 3)  # 32 spins
     csr = native.Csr.from_dense(f)
     beta = native.geometric_schedule(0.2, 3.0, 25)
-    rs = native.anneal_sparse(csr, beta, num_tries=500, sweeps_per_beta=1, acceptance=1, seed=2, ctx=ctx)
-    # Oracle: sequential sweeps in the same colour-sorted order are not
-    # available there; natural order gives the same stationary behaviour.
-    _, e_ref, _ = orc.anneal_free(f, beta, 500, 1, seed=8, acceptance=1, site_order=1)
+    plan = native.AnnealPlan(csr, beta, num_tries=500, acceptance=1, seed=2, ctx=ctx)
+    try:
+        plan.execute()
+        rs = plan.result()
+        order = plan.sweep_order()
+    finally:
+        plan.close()
+    # The oracle's chain in the kernel's colour-sorted sweep order, with the
+    # kernel's sweep-end best-state bookkeeping: the same Markov chain.
+    _, e_ref, _ = orc.anneal_free_fields(f, beta, 500, 1, seed=8, acceptance=1, site_order=1, order=order,
+                                         best_at_sweep_end=True)
     ks = _ks(rs.traj_energies, e_ref)
     assert ks.pvalue > 1e-3, ks
 
