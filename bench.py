@@ -260,7 +260,7 @@ def bench_exhaustive(args, ctx, pg, rank, world):
     import onesolver_gb300 as osg
     n = 36
     f = int_qubo(n, rank)  # seed 0 on rank 0; independent instances on replicas
-    plan = osg.ExhaustivePlan(f, ctx=ctx, max_minimisers=1 << 16)
+    plan = osg.ExhaustivePlan(f, ctx=ctx, max_minimisers=1 << 16, variant=args.exh_variant)
     flush_buf = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
     launches = []
 
@@ -294,8 +294,13 @@ def bench_exhaustive(args, ctx, pg, rank, world):
     d2h = 56 + 8 * min(r.count, 1 << 16)
 
     k_ms = statistics.mean(kern_ms)
-    peak = osg.probe_int32_peak(ctx)
-    achieved = states * 2 / (k_ms * 1e-3) / 1e9
+    # Matched ceiling: the issue rate of the instructions this plan's variant
+    # spends per state (packed variant: two states per add), measured in this
+    # run; MEASURED_PEAKS.json has no integer figure.
+    variant = plan.variant
+    peak = osg.probe_exhaustive_pair(variant, ctx)
+    achieved = states / (k_ms * 1e-3)
+    sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
     out = {
         "metric": "exhaustive enumerated states/s (n=36, int32 Gray code, all degenerate minimisers)",
         "value": value, "unit": "states/s", "ms_per_step": t_step,
@@ -305,11 +310,13 @@ def bench_exhaustive(args, ctx, pg, rank, world):
                    "n": n, "states_per_step": int(states), "l2": "flushed (256 MB write) before every timed step",
                    "parallelism": f"replicas x{world}" if world > 1 else "1 GPU"},
         "result": {"energy": res.energy, "state": res.state, "minimisers": res.count},
-        "roofline": {"bound": "int32-issue", "achieved": achieved, "peak": peak, "unit": "Gop/s",
+        "roofline": {"bound": "int-issue", "achieved": achieved, "peak": peak, "unit": "states/s",
                      "frac": achieved / peak, "traffic": TRAFFIC.get("exhaustive36"),
-                     "ops_per_unit": 2, "kernel_ms": k_ms,
-                     "peak_source": "os_probe_int32_peak: add+min issue rate measured in this run "
-                                    "(MEASURED_PEAKS.json has no INT32 figure)"},
+                     "variant": variant, "ops_per_unit": 2, "kernel_ms": k_ms,
+                     "states_per_sm_clock": achieved / (sms * load_peaks().get("sm_max_mhz", 2070.0) * 1e6),
+                     "peak_source": ("os_probe_exhaustive_pair(%d): the issue rate of this variant's per-state "
+                                     "instructions, measured in this run (MEASURED_PEAKS.json has no integer "
+                                     "figure)" % variant)},
         "e2e": {"value": world * states / e2e_step, "unit": "states/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "ms_per_step": e2e_step * 1e3},
         "gpu_launches": int(sum(launches)),
@@ -769,14 +776,15 @@ PROFILE_CASES = ("exhaustive32", "exhaustive36", "sa-sk1024", "sa-batch48", "sa-
                  "mpnn-predict1024", "pt-droplet512", "pa-droplet512")
 
 
-def profile_case(name: str, ctx) -> None:
+def profile_case(name: str, ctx, exh_variant: int = 0) -> None:
     """One small execution of a hot-path kernel, for ncu captures: inputs
     larger than L2 where the kernel streams them, a few GB on the device at
     most, a handful of launches."""
     import torch
     import onesolver_gb300 as osg
     if name in ("exhaustive32", "exhaustive36"):
-        plan = osg.ExhaustivePlan(int_qubo(int(name[-2:]), 0), ctx=ctx, max_minimisers=1 << 16)
+        plan = osg.ExhaustivePlan(int_qubo(int(name[-2:]), 0), ctx=ctx, max_minimisers=1 << 16,
+                                  variant=exh_variant)
     elif name == "sa-sk1024":
         plan = osg.AnnealPlan(sk_qubo(1024, 0), osg.geometric_schedule(0.1, 5.0, 10), num_tries=512,
                               acceptance=osg.ACCEPT_PHYSICAL, site_order=osg.SITES_SEQUENTIAL, ctx=ctx)
@@ -845,6 +853,8 @@ def main():
                     help="also measure the SA workloads and report them under 'secondary'")
     ap.add_argument("--cpu-baseline", action=argparse.BooleanOptionalAction, default=True)
     ap.add_argument("--ref-budget", type=float, default=8.0, help="seconds of CPU work per reference step")
+    ap.add_argument("--exh-variant", type=int, default=0, choices=[0, 1, 2, 3],
+                    help="exhaustive instruction variant (0 = the library's default)")
     ap.add_argument("--learned-train", type=int, default=256)
     ap.add_argument("--learned-eval", type=int, default=8)
     ap.add_argument("--learned-epochs", type=int, default=20)
@@ -856,7 +866,7 @@ def main():
         import torch
         import onesolver_gb300 as osg
         ctx = osg.Context(0)
-        profile_case(args.profile_case, ctx)
+        profile_case(args.profile_case, ctx, args.exh_variant)
         ctx.close()
         return
     if args.steps <= 0:

@@ -153,9 +153,15 @@ typedef struct os_exh_params {
   uint64_t max_minimisers;  /* capacity of os_exh_result.states */
   int32_t inner_bits;       /* 0 = default (10); 9 or 10 sets how many low
                                bits the unrolled inner loop walks (tuning) */
-  int32_t variant;          /* 0 = default; 1 = three-input add + min per
-                               state; 2 = multiply-add + fused add-min
-                               (int32 only; tuning) */
+  int32_t variant;          /* 0 = default (3 where it applies, else 2);
+                               1 = three-input add + min per state;
+                               2 = multiply-add + fused add-min;
+                               3 = two states per three-input add in 16-bit
+                               halves and a per-half minimum, for int32
+                               coefficients whose magnitudes (upper
+                               triangle) sum to at most 8,000 and
+                               n - fixed_high_bits > inner_bits
+                               (int32 only; every variant is exact) */
 } os_exh_params;
 
 typedef struct os_exh_result {
@@ -197,6 +203,10 @@ os_status os_exhaustive_plan_execute(os_exh_plan *plan);
 os_status os_exhaustive_plan_result(os_exh_plan *plan, os_exh_result *result);
 /* Kernel launches made by the last execute (for launch accounting). */
 int32_t os_exhaustive_plan_launches(const os_exh_plan *plan);
+/* The instruction variant the plan's enumeration runs (os_exh_params.variant
+ * after defaults: 1, 2 or 3; int64 and fixed-point searches report 1); 0
+ * when the space is small enough for one thread per state. */
+int32_t os_exhaustive_plan_variant(const os_exh_plan *plan);
 /* Device time of the last execute's enumeration kernel, from CUDA events
  * recorded on the context's stream around it (waits for it to finish). */
 os_status os_exhaustive_plan_kernel_ms(os_exh_plan *plan, float *ms);
@@ -588,6 +598,13 @@ os_status os_mpnn_predict(os_mpnn *model, const os_qubo_dense *qubo, float *prob
  * and the shared-memory read rate of the annealing field update (128-bit
  * shared loads feeding paired FP32 FMAs), in GB/s. No reference counterpart. */
 os_status os_probe_int32_peak(os_ctx *ctx, double *gops);
+/* States per second at the issue rate of exhaustive variant `variant`'s
+ * per-state instructions (1: three-input add + min; 2: multiply-add + fused
+ * add-min; 3: packed 16-bit halves, a three-input add per two states and a
+ * three-input per-half minimum per four), four independent chains per thread
+ * at full occupancy: the ceiling of the enumeration's inner loop without its
+ * bookkeeping. */
+os_status os_probe_exhaustive_pair(os_ctx *ctx, int32_t variant, double *states_per_s);
 os_status os_probe_fp32_fma_peak(os_ctx *ctx, double *gflops);
 os_status os_probe_smem_row_peak(os_ctx *ctx, double *gbs);
 

@@ -150,6 +150,7 @@ SIGNATURES = {
     "os_exhaustive_plan_execute": (C.c_int, [_P]),
     "os_exhaustive_plan_result": (C.c_int, [_P, C.POINTER(_ExhResult)]),
     "os_exhaustive_plan_launches": (C.c_int32, [_P]),
+    "os_exhaustive_plan_variant": (C.c_int32, [_P]),
     "os_exhaustive_plan_destroy": (None, [_P]),
     "os_exhaustive_plan_kernel_ms": (C.c_int, [_P, C.POINTER(C.c_float)]),
     "os_exhaustive_run_noalloc": (C.c_int, [C.POINTER(_QuboDense), C.POINTER(_ExhParams), C.POINTER(_ExhResult),
@@ -198,6 +199,7 @@ SIGNATURES = {
     "os_mpnn_train": (C.c_int, [_P, C.c_int32, C.c_float, C.c_uint64, C.POINTER(C.c_float)]),
     "os_mpnn_predict": (C.c_int, [_P, C.POINTER(_QuboDense), C.POINTER(C.c_float)]),
     "os_probe_int32_peak": (C.c_int, [_P, C.POINTER(C.c_double)]),
+    "os_probe_exhaustive_pair": (C.c_int, [_P, C.c_int32, C.POINTER(C.c_double)]),
     "os_probe_fp32_fma_peak": (C.c_int, [_P, C.POINTER(C.c_double)]),
     "os_probe_smem_row_peak": (C.c_int, [_P, C.POINTER(C.c_double)]),
 }
@@ -474,6 +476,11 @@ class ExhaustivePlan:
     @property
     def launches(self) -> int:
         return int(lib().os_exhaustive_plan_launches(self._h))
+
+    @property
+    def variant(self) -> int:
+        """Instruction variant of the enumeration (0: one thread per state)."""
+        return int(lib().os_exhaustive_plan_variant(self._h))
 
     def kernel_ms(self) -> float:
         """Device time of the last execute's enumeration kernel (CUDA events)."""
@@ -1084,6 +1091,15 @@ def probe_int32_peak(ctx: Optional[Context] = None) -> float:
     v = C.c_double()
     _check(lib().os_probe_int32_peak(ctx.handle, C.byref(v)))
     return v.value
+
+
+def probe_exhaustive_pair(variant: int, ctx: Optional[Context] = None) -> float:
+    """States/s at the issue rate of exhaustive variant `variant`'s per-state
+    instructions (1, 2 or 3; 3 = packed, two states per add)."""
+    ctx = ctx or default_context()
+    v = C.c_double()
+    _check(lib().os_probe_exhaustive_pair(ctx.handle, variant, C.byref(v)))
+    return float(v.value)
 
 
 def probe_fp32_fma_peak(ctx: Optional[Context] = None) -> float:

@@ -9,7 +9,7 @@
 // Here the 2^n states are enumerated in Gray-code order so that consecutive
 // states differ in one bit and the energy changes by one precomputed delta:
 //
-//   * the low G bits ("inner" bits, G = 8..10, 9 by default) are walked by
+//   * the low G bits ("inner" bits, G = 9 or 10, 10 by default) are walked by
 //     fully unrolled code.
 //     For step t of the inner Gray sequence the flipped bit k = ctz(t) and
 //     its direction are compile-time constants, so the energy update is
@@ -212,6 +212,25 @@ namespace {
 //                  [7] pruning bound (best energy published so far)
 enum { C_WORK = 0, C_OUT_COUNT, C_OUT_POS, C_OUT_MIN, C_CAND_COUNT, C_CAND_POS, C_CAND_MIN, C_GBEST, C_N };
 
+// The instruction variant a search runs (os_exh_params.variant): the
+// caller's, else the packed variant where it is exact (int32 coefficients
+// whose magnitudes sum to at most PACK_MAX_ABS, and at least one loop bit to
+// split an item's blocks into pairs), else the fused pair. int64 and
+// fixed-point searches run MODE 0 whatever the variant.
+int choose_variant(int requested, int kind, double abs_sum, bool small, int free_bits, int G) {
+  const bool packable = kind == OS_COEF_INT32 && !small && abs_sum <= PACK_MAX_ABS &&
+                        std::min(LOOP_BITS, free_bits - G) >= 1;
+  if (requested == OS_EXH_VARIANT_PACKED)
+    OS_REQUIRE(packable, "variant 3 (packed) needs int32 coefficients whose magnitudes sum to at most %g "
+               "and more than %d free bits", PACK_MAX_ABS, G);
+  if (requested) return requested;
+  return packable ? OS_EXH_VARIANT_PACKED : OS_EXH_VARIANT_DEFAULT;
+}
+
+// v in both 16-bit halves of a word: v * 65537 mod 2^32, the packed form of
+// the pair (v, v) (the packed variant's constants).
+inline int pack2(long long v) { return (int)((uint32_t)v * 65537u); }
+
 // Inner step constants for width G: kf[t] = +/- (Q_kk + sum of Q_kj over
 // the other inner bits set before step t), k = ctz(t).
 template <class T> void inner_constants(const T *q, int n, int G, T *kf) {
@@ -224,6 +243,31 @@ template <class T> void inner_constants(const T *q, int n, int G, T *kf) {
     for (int j = 0; j < G; ++j)
       if (j != k && ((prev >> j) & 1)) base += q[(size_t)k * n + j];
     kf[t] = up ? base : -base;
+  }
+}
+
+// Step constants of the packed variant (GrayParams::kp, qs) for width G.
+template <class T> void packed_constants(const T *q, int n, int G, const T *kf, GrayParams<T> &P) {
+  for (int t = 0; t < INNER_MAX; ++t) P.kp[t] = 0;
+  for (int j = 0; j < (INNER_MAX >> SUB_BITS); ++j)
+    for (int i = 0; i < SUB_BITS; ++i) P.qs[j][i] = 0;
+  if (G <= SUB_BITS) return;
+  for (int t = 1; t < (1 << G); ++t) {
+    const int k = ctz_c(t);
+    const int prev = gray_c(t - 1);
+    const bool up = (gray_c(t) >> k) & 1;
+    if (k < SUB_BITS) {
+      T base = q[(size_t)k * n + k];
+      for (int j = 0; j < SUB_BITS; ++j)
+        if (j != k && ((prev >> j) & 1)) base += q[(size_t)k * n + j];
+      P.kp[t] = pack2(up ? base : -base);
+    } else {
+      P.kp[t] = pack2(kf[t]);
+      for (int i = 0; i < SUB_BITS; ++i) {
+        const T v = q[(size_t)k * n + i];
+        P.qs[t >> SUB_BITS][i] = pack2(up ? v : -v);
+      }
+    }
   }
 }
 
@@ -243,6 +287,7 @@ void fill_params(os_exh_plan *p, GrayParams<T> &P, const std::vector<T> &q,
     acc += kf[t];
     P.ks[t] = acc;
   }
+  if (!p->small) packed_constants(q.data(), n, p->G, kf.data(), P);
   P.one = 1;
   P.q = dq.get();
   P.kf_g = dkf.get();
@@ -285,13 +330,13 @@ void launch_gray(int G, int variant, int grid, cudaStream_t s, const GrayParams<
     throw_error(OS_INVALID_ARG, "inner_bits must be 9 or 10");
 }
 
-template <class T> int gray_occupancy(int G) {
-  return G == 9 ? gray_occupancy_width<T, 9>() : gray_occupancy_width<T, 10>();
+template <class T> int gray_occupancy(int G, int variant) {
+  return G == 9 ? gray_occupancy_width<T, 9>(variant) : gray_occupancy_width<T, 10>(variant);
 }
 
 template <class T> int grid_for(os_exh_plan *p, const GrayParams<T> &P) {
   if (p->small) return (int)ceil_div_u64(P.nstates, THREADS);
-  const int occ = gray_occupancy<T>(p->G);
+  const int occ = gray_occupancy<T>(p->G, p->variant);
   const unsigned long long items = 1ull << P.item_bits;
   const unsigned long long want = ceil_div_u64(items, THREADS);
   return (int)std::max<unsigned long long>(1, std::min<unsigned long long>(want, (unsigned long long)p->ctx->sm_count * occ));
@@ -401,7 +446,7 @@ os_status os_exhaustive_plan_create(os_ctx *ctx, const os_qubo_dense *qubo,
     OS_REQUIRE(kind >= OS_COEF_INT32 && kind <= OS_COEF_FIXED64, "unknown coef_kind %d", kind);
     OS_REQUIRE(prm.inner_bits == 0 || prm.inner_bits == 9 || prm.inner_bits == 10,
                "inner_bits must be 0 (default), 9 or 10");
-    OS_REQUIRE(prm.variant >= 0 && prm.variant <= OS_EXH_VARIANT_FUSED, "unknown variant %d", prm.variant);
+    OS_REQUIRE(prm.variant >= 0 && prm.variant <= OS_EXH_VARIANT_PACKED, "unknown variant %d", prm.variant);
     if (kind == OS_COEF_INT32)
       OS_REQUIRE(integral && abs_sum < 2147483000.0, "coefficients are not int32-exact");
     if (kind == OS_COEF_INT64)
@@ -417,7 +462,7 @@ os_status os_exhaustive_plan_create(os_ctx *ctx, const os_qubo_dense *qubo,
       p->kind = kind;
       p->small = p->free_bits < SMALL_FREE;
       p->G = prm.inner_bits ? prm.inner_bits : G_DEFAULT;
-      p->variant = prm.variant ? prm.variant : OS_EXH_VARIANT_DEFAULT;
+      p->variant = choose_variant(prm.variant, kind, abs_sum, p->small, p->free_bits, p->G);
       p->prefix_state = prm.fixed_high_bits ? (prm.prefix << p->free_bits) : 0ull;
       p->user_cap = prm.max_minimisers;
       p->out_cap = std::max<unsigned long long>(prm.max_minimisers, 1ull);
@@ -483,6 +528,11 @@ os_status os_exhaustive_plan_execute(os_exh_plan *p) {
 }
 
 int32_t os_exhaustive_plan_launches(const os_exh_plan *p) { return p ? p->launches : 0; }
+
+int32_t os_exhaustive_plan_variant(const os_exh_plan *p) {
+  if (!p || p->small) return 0;
+  return p->kind == OS_COEF_INT32 ? p->variant : OS_EXH_VARIANT_ADD_MIN;
+}
 
 os_status os_exhaustive_plan_result(os_exh_plan *p, os_exh_result *r) {
   os_status extra = OS_OK;
@@ -637,7 +687,7 @@ unsigned char *noalloc_scratch(int device) {
 
 template <class T>
 void noalloc_run(const os_qubo_dense *qubo, const os_exh_params &prm, os_exh_result *r, int kind,
-                 cudaStream_t s, int device, unsigned char *base) {
+                 double abs_sum, cudaStream_t s, int device, unsigned char *base) {
   const int n = qubo->n;
   const int free_bits = n - prm.fixed_high_bits;
   const bool small = free_bits < SMALL_FREE;
@@ -649,7 +699,7 @@ void noalloc_run(const os_qubo_dense *qubo, const os_exh_params &prm, os_exh_res
   // Inner width and instruction variant as os_exhaustive_plan_create
   // chooses them (the caller's values, else the defaults).
   const int G = prm.inner_bits ? prm.inner_bits : G_DEFAULT;
-  const int variant = prm.variant ? prm.variant : OS_EXH_VARIANT_DEFAULT;
+  const int variant = choose_variant(prm.variant, kind, abs_sum, small, free_bits, G);
   GrayParams<T> P{};
   T kf[INNER_MAX];
   if (!small) inner_constants(q, n, G, kf);
@@ -660,6 +710,7 @@ void noalloc_run(const os_qubo_dense *qubo, const os_exh_params &prm, os_exh_res
     acc += kf[t];
     P.ks[t] = acc;
   }
+  if (!small) packed_constants(q, n, G, kf, P);
   P.one = 1;
   unsigned long long *counters = reinterpret_cast<unsigned long long *>(base + NA_COUNTERS);
   Summary *summary = reinterpret_cast<Summary *>(base + NA_SUMMARY);
@@ -696,7 +747,7 @@ void noalloc_run(const os_qubo_dense *qubo, const os_exh_params &prm, os_exh_res
     ctas = (int)ceil_div_u64(P.nstates, THREADS);
   } else {
     int occ = 0, sms = 0;
-    occ = gray_occupancy<T>(G);
+    occ = gray_occupancy<T>(G, variant);
     OS_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
     const unsigned long long want = ceil_div_u64(1ull << P.item_bits, THREADS);
     ctas = (int)std::min<unsigned long long>(want, (unsigned long long)sms * std::max(occ, 1));
@@ -773,7 +824,7 @@ extern "C" os_status os_exhaustive_run_noalloc(const os_qubo_dense *qubo, const 
       OS_REQUIRE(prm.prefix == 0, "prefix given without fixed_high_bits");
     OS_REQUIRE(prm.inner_bits == 0 || prm.inner_bits == 9 || prm.inner_bits == 10,
                "inner_bits must be 0 (default), 9 or 10");
-    OS_REQUIRE(prm.variant >= 0 && prm.variant <= OS_EXH_VARIANT_FUSED, "unknown variant %d", prm.variant);
+    OS_REQUIRE(prm.variant >= 0 && prm.variant <= OS_EXH_VARIANT_PACKED, "unknown variant %d", prm.variant);
     OS_REQUIRE(prm.max_minimisers <= NOALLOC_MAX_OUT,
                "max_minimisers %llu exceeds the no-allocation limit of %llu",
                (unsigned long long)prm.max_minimisers, (unsigned long long)NOALLOC_MAX_OUT);
@@ -798,9 +849,9 @@ extern "C" os_status os_exhaustive_run_noalloc(const os_qubo_dense *qubo, const 
     unsigned char *base = noalloc_scratch(device);
     cudaStream_t s = (cudaStream_t)stream;
     if (kind == OS_COEF_INT32)
-      noalloc_run<int>(qubo, prm, result, kind, s, device, base);
+      noalloc_run<int>(qubo, prm, result, kind, abs_sum, s, device, base);
     else
-      noalloc_run<long long>(qubo, prm, result, kind, s, device, base);
+      noalloc_run<long long>(qubo, prm, result, kind, abs_sum, s, device, base);
     if (prm.max_minimisers > 0 && result->count > prm.max_minimisers) extra = OS_OVERFLOW_MINIMISERS;
   });
   if (st != OS_OK) return st;

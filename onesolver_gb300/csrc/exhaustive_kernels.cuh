@@ -19,7 +19,14 @@ namespace exh {
 constexpr int G_DEFAULT = 10;        // inner (unrolled) bits
 constexpr int OS_EXH_VARIANT_ADD_MIN = 1;  // three-input add + min (ALU pipe)
 constexpr int OS_EXH_VARIANT_FUSED = 2;    // FMA-pipe multiply-add + fused add-min
+constexpr int OS_EXH_VARIANT_PACKED = 3;   // two states per add in 16-bit halves, register sub-walk
 constexpr int OS_EXH_VARIANT_DEFAULT = OS_EXH_VARIANT_FUSED;
+// Packed variant: each half holds energy + PACK_BIAS in [0, 32767]; safe when
+// the coefficient magnitudes (upper triangle) sum to at most PACK_MAX_ABS, so
+// that every energy and every coupling sum stays within 16383.
+constexpr int PACK_BIAS = 16384;
+constexpr double PACK_MAX_ABS = 8000.0;
+constexpr int SUB_BITS = 4;          // packed variant: inner bits walked against registers
 constexpr int G_MAX = 10;
 constexpr int INNER_MAX = 1 << G_MAX;
 constexpr int LCAP = 4;              // states kept per thread
@@ -57,6 +64,12 @@ struct Summary {
 template <class T> struct GrayParams {
   T kf[INNER_MAX];                // inner step constants (kf[0] unused)
   T ks[INNER_MAX];                // prefix sums ks[t] = kf[1] + ... + kf[t]
+  // Packed variant (both halves, i.e. times 65537): step t flipping a sub
+  // bit k < SUB_BITS adds kp[t] = +/-(Q_kk + couplings to the set sub bits);
+  // a step flipping k >= SUB_BITS adds kp[t] = kf[t] and moves the sub bits'
+  // outside couplings by qs[t / 2^SUB_BITS][i] = +/- Q_ki.
+  int kp[INNER_MAX];
+  int qs[INNER_MAX >> SUB_BITS][SUB_BITS];
   T one;                          // 1, as a runtime value
   const T *q;                     // n x n symmetric coefficients
   const T *kf_g;                  // global copy of kf (slow path)
@@ -94,6 +107,7 @@ template <> __device__ __forceinline__ long long tmax<long long>() { return LLON
 //           a runtime +/-1 (an integer multiply-add, which issues on the FMA
 //           pipe), and the energy E + ks[t] meets the minimum in one fused
 //           add-min; the ALU pipe then carries one instruction per state.
+//   (MODE 2, the packed variant, has its own block walk: inner_block_packed.)
 template <class T, int G, int MODE, int t>
 __device__ __forceinline__ void inner_step(T &E, T &m, const T (&c)[G], const GrayParams<T> &P, T pos,
                                            T neg) {
@@ -106,6 +120,60 @@ __device__ __forceinline__ void inner_step(T &E, T &m, const T (&c)[G], const Gr
     E = c[k] * (up ? pos : neg) + E;
     m = __viaddmin_s32(E, P.ks[t], m);
   }
+}
+
+// MODE 2: one block of 2^G inner states for two walks at once. E, c and cs
+// hold two values as x_b * 65536 + x_a, both energies biased into
+// [0, 32767], so plain 32-bit adds update both halves exactly (a packed sum
+// is a sum of packed values) and the per-half minimum is one 16x2
+// instruction. The low SUB_BITS inner bits are walked against cs[], their
+// couplings to every set bit outside them, kept in registers and moved at the
+// steps that flip a higher bit; every state then costs one three-input add
+// whose constant comes from the parameter bank, and every two states one
+// three-input per-half minimum.
+template <int G, int t>
+__device__ __forceinline__ void packed_step(int &E, int (&cs)[SUB_BITS], const int (&c)[G],
+                                            const GrayParams<int> &P) {
+  constexpr int k = ctz_c(t);
+  constexpr bool up = (gray_c(t) >> k) & 1;
+  if constexpr (k < SUB_BITS) {
+    E = E + P.kp[t] + (up ? cs[k] : -cs[k]);
+  } else {
+    E = E + P.kp[t] + (up ? c[k] : -c[k]);
+#pragma unroll
+    for (int i = 0; i < SUB_BITS; ++i) cs[i] += P.qs[t >> SUB_BITS][i];
+  }
+}
+
+template <int G, int t>
+__device__ __forceinline__ void packed_pair(int &E, int &m, int (&cs)[SUB_BITS], const int (&c)[G],
+                                            const GrayParams<int> &P) {
+  packed_step<G, t>(E, cs, c, P);
+  if constexpr (t + 1 < (1 << G)) {
+    const int e1 = E;
+    packed_step<G, t + 1>(E, cs, c, P);
+    m = (int)__vimin3_s16x2((unsigned)m, (unsigned)e1, (unsigned)E);
+  } else {
+    m = (int)__vimin3_s16x2((unsigned)m, (unsigned)E, (unsigned)E);
+  }
+}
+
+template <int G, int... Is>
+__device__ __forceinline__ void packed_block_impl(int &E, int &m, int (&cs)[SUB_BITS], const int (&c)[G],
+                                                  const GrayParams<int> &P, std::integer_sequence<int, Is...>) {
+  (packed_pair<G, 2 * Is + 1>(E, m, cs, c, P), ...);
+}
+
+// Minimum (per half) over the block that starts at packed energy E with
+// packed outer couplings c.
+template <int G>
+__device__ __forceinline__ int inner_block_packed(int E, const int (&c)[G], const GrayParams<int> &P) {
+  int cs[SUB_BITS];
+#pragma unroll
+  for (int i = 0; i < SUB_BITS; ++i) cs[i] = c[i];
+  int m = E;
+  packed_block_impl<G>(E, m, cs, c, P, std::make_integer_sequence<int, (1 << (G - 1))>{});
+  return m;
 }
 
 template <class T, int G, int MODE, int... Is>
@@ -193,39 +261,65 @@ __device__ __forceinline__ void collect_state(CollectState &cs, const GrayParams
 // per-thread pruning bound so that blocks are walked again only when they
 // reach the best energy known (a warp pays for the slow walk whenever any of
 // its lanes needs it).
+//
+// The 32 lanes of a warp run one descent together: lane l keeps the local
+// fields of variables l and l + 32, and each step's flip (the largest
+// decrease, the lowest index among equals) comes from a warp argmin, so a
+// descent costs O(n) steps of a few instructions per lane instead of O(n^2)
+// serial work per thread. Every lane returns the same energy.
 template <class T>
-__device__ __noinline__ T descent_bound(const GrayParams<T> &P, uint32_t tid) {
+__device__ __noinline__ T descent_bound_warp(const GrayParams<T> &P, uint32_t wid) {
+  const int lane = threadIdx.x & 31;
   const int n = P.n;
   const T *__restrict__ q = P.q;
-  const Philox4 r = philox4x32_10(tid, 0u, 0u, 0xE5000000u, P.seed, 0x9E3779B9u);
+  const Philox4 r = philox4x32_10(wid, 1u, 0u, 0xE5000000u, P.seed, 0x9E3779B9u);
   const unsigned long long rnd = ((unsigned long long)r.x << 32) | r.y;
   unsigned long long x = P.prefix_state | (rnd & ~P.fixed_mask & P.var_mask);
-  T h[MAX_N];
-  for (int j = 0; j < n; ++j) {
-    T a = 0;
-    for (int i = 0; i < n; ++i)
-      if (i != j && ((x >> i) & 1ull)) a += q[(size_t)j * n + i];
-    h[j] = a;
+  const int j0 = lane, j1 = lane + 32;
+  const bool v0 = j0 < n && !((P.fixed_mask >> j0) & 1ull);
+  const bool v1 = j1 < n && !((P.fixed_mask >> j1) & 1ull);
+  T h0 = 0, h1 = 0;
+  for (int i = 0; i < n; ++i) {
+    if (!((x >> i) & 1ull)) continue;
+    if (j0 < n && i != j0) h0 += q[(size_t)j0 * n + i];
+    if (j1 < n && i != j1) h1 += q[(size_t)j1 * n + i];
   }
   T E = energy_from_scratch(q, n, x);
   for (int it = 0; it < 4 * n; ++it) {
-    T best_d = 0;
-    int best_i = -1;
-    for (int i = 0; i < n; ++i) {
-      if ((P.fixed_mask >> i) & 1ull) continue;
-      const T loc = q[(size_t)i * n + i] + h[i];
-      const T d = ((x >> i) & 1ull) ? -loc : loc;
-      if (d < best_d) {
-        best_d = d;
-        best_i = i;
+    T bd = 0;
+    int bi = INT_MAX;
+    if (v0) {
+      const T loc = q[(size_t)j0 * n + j0] + h0;
+      const T d = ((x >> j0) & 1ull) ? -loc : loc;
+      if (d < bd) {
+        bd = d;
+        bi = j0;
       }
     }
-    if (best_i < 0) break;
-    const bool was = (x >> best_i) & 1ull;
-    x ^= 1ull << best_i;
-    E += best_d;
-    for (int j = 0; j < n; ++j)
-      if (j != best_i) h[j] += was ? -q[(size_t)best_i * n + j] : q[(size_t)best_i * n + j];
+    if (v1) {
+      const T loc = q[(size_t)j1 * n + j1] + h1;
+      const T d = ((x >> j1) & 1ull) ? -loc : loc;
+      if (d < bd) {
+        bd = d;
+        bi = j1;
+      }
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+      const T od = __shfl_xor_sync(0xffffffffu, bd, off);
+      const int oi = __shfl_xor_sync(0xffffffffu, bi, off);
+      if (od < bd || (od == bd && oi < bi)) {
+        bd = od;
+        bi = oi;
+      }
+    }
+    if (bi == INT_MAX) break;  // warp-uniform: no flip lowers the energy
+    const bool was = (x >> bi) & 1ull;
+    x ^= 1ull << bi;
+    E += bd;
+    const T *row = q + (size_t)bi * n;
+    if (j0 < n && j0 != bi) h0 += was ? -row[j0] : row[j0];
+    if (j1 < n && j1 != bi) h1 += was ? -row[j1] : row[j1];
   }
   return E;
 }
@@ -322,6 +416,97 @@ __device__ __forceinline__ void process_item(unsigned long long item, const Gray
   }
 }
 
+// MODE 2: an item's 2^loop_bits blocks as 2^(loop_bits-1) pairs walked
+// together: half a has the top loop bit (`top`) clear, half b set; the two
+// flip the same outer bits (all below `top`), so one row sum serves both and
+// the coupling vectors and block-start energies stay packed between blocks
+// (x_b * 65536 + x_a; c_b = c_a + Q[top][.]). A block pair whose smaller
+// half-minimum reaches the bound is walked again state by state, each half
+// that reaches it on its own, exactly as MODE 1 does.
+template <int G>
+__device__ __forceinline__ void process_item_packed(unsigned long long item, const GrayParams<int> &P,
+                                                    ThreadBest<int> &tb, CollectState &cs) {
+  const int n = P.n;
+  const int *__restrict__ q = P.q;
+  const int top = G + P.loop_bits - 1;
+  const int *__restrict__ rowt = q + (size_t)top * n;
+  unsigned long long xa = P.prefix_state | (item << (G + P.loop_bits));
+  const int Ea = energy_from_scratch(q, n, xa);
+  int ca[G];
+#pragma unroll
+  for (int i = 0; i < G; ++i) ca[i] = 0;
+  int sumt = rowt[top];
+  {
+    unsigned long long r = xa;
+    while (r) {
+      const int j = __ffsll((long long)r) - 1;
+      r &= r - 1;
+      const int *row = q + (size_t)j * n;
+#pragma unroll
+      for (int i = 0; i < G; ++i) ca[i] += row[i];
+      sumt += rowt[j];
+    }
+  }
+  int c2[G];
+#pragma unroll
+  for (int i = 0; i < G; ++i) c2[i] = (ca[i] + rowt[i]) * 65536 + ca[i];
+  int E2s = (Ea + sumt + PACK_BIAS) * 65536 + (Ea + PACK_BIAS);
+  const unsigned npairs = 1u << (P.loop_bits - 1);
+  for (unsigned B = 0; B < npairs; ++B) {
+    const int m = inner_block_packed<G>(E2s, c2, P);
+    if ((B & 7u) == 7u) {
+      const long long g = *reinterpret_cast<volatile long long *>(P.gbest);
+      if (g < (long long)tb.best) {
+        tb.best = (int)g;
+        tb.cnt = 0;
+        tb.minstate = ~0ull;
+      }
+    }
+    const int ma = (int)((unsigned)m & 0xFFFFu) - PACK_BIAS;
+    const int mb = (int)((unsigned)m >> 16) - PACK_BIAS;
+    const int mm = min(ma, mb);
+    if (mm <= tb.best) {
+      if (mm < tb.best) {
+        tb.best = mm;
+        tb.cnt = 0;
+        tb.minstate = ~0ull;
+        atomicMin(P.gbest, (long long)mm);
+      }
+      CVec<int, G> cv;
+      if (ma <= tb.best) {
+#pragma unroll
+        for (int i = 0; i < G; ++i) cv.v[i] = (int)(short)(c2[i] & 0xFFFF);
+        revisit_block<int, G, false>(P, cv, xa, (int)((unsigned)E2s & 0xFFFFu) - PACK_BIAS, tb, cs, 0);
+      }
+      if (mb <= tb.best) {
+#pragma unroll
+        for (int i = 0; i < G; ++i) cv.v[i] = (c2[i] - (int)(short)(c2[i] & 0xFFFF)) >> 16;
+        revisit_block<int, G, false>(P, cv, xa | (1ull << top), (int)((unsigned)E2s >> 16) - PACK_BIAS, tb, cs,
+                                     0);
+      }
+    }
+    if (B + 1 < npairs) {
+      const int mbit = G + __ffs((int)(B + 1)) - 1;
+      const unsigned long long bm = 1ull << mbit;
+      const bool was = (xa & bm) != 0;
+      const int *row = q + (size_t)mbit * n;
+      int sum = row[mbit];
+      unsigned long long r = xa & ~bm;
+      while (r) {
+        const int j = __ffsll((long long)r) - 1;
+        r &= r - 1;
+        sum += row[j];
+      }
+      const int sum2 = sum * 65537 + row[top] * 65536;  // half b also has `top` set
+      E2s += was ? -sum2 : sum2;
+      xa ^= bm;
+      const int s65537 = was ? -65537 : 65537;
+#pragma unroll
+      for (int i = 0; i < G; ++i) c2[i] += row[i] * s65537;
+    }
+  }
+}
+
 // CTA reduction of the per-thread bests into one record per CTA.
 template <class T>
 __device__ __forceinline__ void cta_reduce(const GrayParams<T> &P, ThreadBest<T> &tb) {
@@ -380,8 +565,9 @@ __global__ void __launch_bounds__(THREADS) gray_kernel(const __grid_constant__ G
     __shared__ long long s_bound;
     if (threadIdx.x == 0) s_bound = LLONG_MAX;
     __syncthreads();
-    const T d = descent_bound(P, blockIdx.x * blockDim.x + threadIdx.x);
-    atomicMin(&s_bound, (long long)d);
+    const uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const T d = min(descent_bound_warp(P, 2 * w), descent_bound_warp(P, 2 * w + 1));
+    if ((threadIdx.x & 31) == 0) atomicMin(&s_bound, (long long)d);
     __syncthreads();
     if (threadIdx.x == 0) atomicMin(P.gbest, s_bound);
     const long long g = *reinterpret_cast<volatile long long *>(P.gbest);
@@ -395,7 +581,12 @@ __global__ void __launch_bounds__(THREADS) gray_kernel(const __grid_constant__ G
     base = __shfl_sync(0xffffffffu, base, 0);
     if (base >= items) break;
     const unsigned long long item = base + lane;
-    if (item < items) process_item<T, G, COLLECT, MODE>(item, P, tb, cs, thr);
+    if (item < items) {
+      if constexpr (MODE == 2)
+        process_item_packed<G>(item, P, tb, cs);
+      else
+        process_item<T, G, COLLECT, MODE>(item, P, tb, cs, thr);
+    }
   }
   if (COLLECT) {
     if (cs.count) {
@@ -412,7 +603,7 @@ __global__ void __launch_bounds__(THREADS) gray_kernel(const __grid_constant__ G
 // exhaustive_gray_l10.cu.
 template <class T, int G> void launch_gray_width(int variant, bool collect, int grid, cudaStream_t s,
                                                   const GrayParams<T> &P);
-template <class T, int G> int gray_occupancy_width();
+template <class T, int G> int gray_occupancy_width(int variant);
 
 }  // namespace exh
 }  // namespace os

@@ -1,9 +1,11 @@
 // probe.cu -- measured roofline denominators that the driver does not
-// provide: the INT32 issue rate of the exhaustive kernel's per-state
-// instruction pair (three-input add with a constant-bank operand, then an
-// integer min), the FP32 FMA rate, and the shared-memory read rate of the
-// dense annealing row update (one 128-bit shared load feeding two paired FP32
-// FMAs per lane, the instruction pair of a field update).
+// provide: the issue rate of the instructions each exhaustive variant spends
+// per state (three-input add with a constant-bank operand and an integer
+// min; multiply-add and fused add-min; packed 16-bit halves, a three-input
+// add per two states and a three-input per-half min per four), the FP32 FMA
+// rate, and the shared-memory read rate of the dense annealing row update
+// (one 128-bit shared load feeding two paired FP32 FMAs per lane, the
+// instruction pair of a field update).
 #include <cstdint>
 #include <utility>
 
@@ -48,6 +50,65 @@ __global__ void __launch_bounds__(256) int32_probe_kernel(const __grid_constant_
   }
   for (int it = 0; it < P.iters; ++it) {
     steps(E, m, c, P, std::make_integer_sequence<int, STEPS>{});
+#pragma unroll
+    for (int j = 0; j < CHAINS; ++j) c[j] ^= m[j] & 1;
+  }
+  int r = 0;
+#pragma unroll
+  for (int j = 0; j < CHAINS; ++j) r ^= m[j] ^ E[j];
+  if (r == 0x7fffffff) P.sink[0] = r;
+}
+
+// The per-state instructions of exhaustive variant V (1: three-input add +
+// min; 2: multiply-add + fused add-min; 3: packed 16-bit halves, one
+// three-input add per two states and one three-input per-half min per four),
+// STEPS steps of CHAINS independent chains per thread; the step constants
+// come from the parameter bank as in the enumeration kernel.
+struct PairParams {
+  int k[STEPS];
+  int k2s[STEPS];
+  int iters;
+  int *sink;
+};
+
+template <int V, int I>
+__device__ __forceinline__ void pair_step(int (&E)[CHAINS], int (&m)[CHAINS], const int (&c)[CHAINS],
+                                          const PairParams &P, int pos, int neg) {
+#pragma unroll
+  for (int j = 0; j < CHAINS; ++j) {
+    if constexpr (V == 1) {
+      E[j] += P.k[I] + ((I & 1) ? c[j] : -c[j]);
+      m[j] = min(m[j], E[j]);
+    } else if constexpr (V == 2) {
+      E[j] = c[j] * ((I & 1) ? pos : neg) + E[j];
+      m[j] = __viaddmin_s32(E[j], P.k[I], m[j]);
+    } else {
+      const int e1 = E[j];
+      E[j] = E[j] + P.k2s[I] + ((I & 2) ? c[j] : -c[j]);
+      if (I & 1) m[j] = (int)__vimin3_s16x2((unsigned)m[j], (unsigned)e1, (unsigned)E[j]);
+    }
+  }
+}
+
+template <int V, int... Is>
+__device__ __forceinline__ void pair_steps(int (&E)[CHAINS], int (&m)[CHAINS], const int (&c)[CHAINS],
+                                           const PairParams &P, int pos, int neg,
+                                           std::integer_sequence<int, Is...>) {
+  (pair_step<V, Is>(E, m, c, P, pos, neg), ...);
+}
+
+template <int V>
+__global__ void __launch_bounds__(256) pair_probe_kernel(const __grid_constant__ PairParams P) {
+  int E[CHAINS], m[CHAINS], c[CHAINS];
+  const int pos = P.k[0] | 1, neg = -pos;  // runtime +-1 (k[0] = 1)
+#pragma unroll
+  for (int j = 0; j < CHAINS; ++j) {
+    E[j] = threadIdx.x * 7 + j;
+    m[j] = 1 << 30;
+    c[j] = (blockIdx.x + j) & 3;
+  }
+  for (int it = 0; it < P.iters; ++it) {
+    pair_steps<V>(E, m, c, P, pos, neg, std::make_integer_sequence<int, STEPS>{});
 #pragma unroll
     for (int j = 0; j < CHAINS; ++j) c[j] ^= m[j] & 1;
   }
@@ -145,6 +206,33 @@ os_status os_probe_int32_peak(os_ctx *ctx, double *gops) {
     });
     const double ops = 2.0 * STEPS * CHAINS * (double)P.iters * grid * 256.0;
     *gops = ops / (ms * 1e-3) / 1e9;
+  });
+}
+
+os_status os_probe_exhaustive_pair(os_ctx *ctx, int32_t variant, double *states_per_s) {
+  return guard([&] {
+    activate(ctx);
+    OS_REQUIRE(states_per_s != nullptr, "null output");
+    OS_REQUIRE(variant >= 1 && variant <= 3, "variant must be 1, 2 or 3");
+    DevBuf<int> sink;
+    sink.alloc(1);
+    PairParams P{};
+    for (int i = 0; i < STEPS; ++i) {
+      P.k[i] = i == 0 ? 1 : (int)((i * 2654435761u) & 15);
+      P.k2s[i] = (int)((uint32_t)P.k[i] * 0x10001u);
+    }
+    P.iters = 64;
+    P.sink = sink.get();
+    auto kern = variant == 1 ? pair_probe_kernel<1> : variant == 2 ? pair_probe_kernel<2> : pair_probe_kernel<3>;
+    int occ = 0;
+    OS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, 256, 0));
+    const int grid = ctx->sm_count * (occ > 0 ? occ : 1);
+    const double ms = time_ms(ctx->stream, [&] {
+      kern<<<grid, 256, 0, ctx->stream>>>(P);
+      OS_CUDA(cudaGetLastError());
+    });
+    const double steps = (double)STEPS * CHAINS * (double)P.iters * grid * 256.0;
+    *states_per_s = steps * (variant == 3 ? 2.0 : 1.0) / (ms * 1e-3);
   });
 }
 
