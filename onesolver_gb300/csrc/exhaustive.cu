@@ -246,29 +246,9 @@ template <class T> void inner_constants(const T *q, int n, int G, T *kf) {
   }
 }
 
-// Step constants of the packed variant (GrayParams::kp, qs) for width G.
-template <class T> void packed_constants(const T *q, int n, int G, const T *kf, GrayParams<T> &P) {
-  for (int t = 0; t < INNER_MAX; ++t) P.kp[t] = 0;
-  for (int j = 0; j < (INNER_MAX >> SUB_BITS); ++j)
-    for (int i = 0; i < SUB_BITS; ++i) P.qs[j][i] = 0;
-  if (G <= SUB_BITS) return;
-  for (int t = 1; t < (1 << G); ++t) {
-    const int k = ctz_c(t);
-    const int prev = gray_c(t - 1);
-    const bool up = (gray_c(t) >> k) & 1;
-    if (k < SUB_BITS) {
-      T base = q[(size_t)k * n + k];
-      for (int j = 0; j < SUB_BITS; ++j)
-        if (j != k && ((prev >> j) & 1)) base += q[(size_t)k * n + j];
-      P.kp[t] = pack2(up ? base : -base);
-    } else {
-      P.kp[t] = pack2(kf[t]);
-      for (int i = 0; i < SUB_BITS; ++i) {
-        const T v = q[(size_t)k * n + i];
-        P.qs[t >> SUB_BITS][i] = pack2(up ? v : -v);
-      }
-    }
-  }
+// Step constants of the packed variant: kf[t] in both halves.
+template <class T> void packed_constants(const T *kf, GrayParams<T> &P) {
+  for (int t = 0; t < INNER_MAX; ++t) P.kp[t] = pack2(kf[t]);
 }
 
 template <class T>
@@ -287,7 +267,7 @@ void fill_params(os_exh_plan *p, GrayParams<T> &P, const std::vector<T> &q,
     acc += kf[t];
     P.ks[t] = acc;
   }
-  if (!p->small) packed_constants(q.data(), n, p->G, kf.data(), P);
+  packed_constants(kf.data(), P);
   P.one = 1;
   P.q = dq.get();
   P.kf_g = dkf.get();
@@ -710,7 +690,7 @@ void noalloc_run(const os_qubo_dense *qubo, const os_exh_params &prm, os_exh_res
     acc += kf[t];
     P.ks[t] = acc;
   }
-  if (!small) packed_constants(q, n, G, kf, P);
+  packed_constants(kf, P);
   P.one = 1;
   unsigned long long *counters = reinterpret_cast<unsigned long long *>(base + NA_COUNTERS);
   Summary *summary = reinterpret_cast<Summary *>(base + NA_SUMMARY);

@@ -19,14 +19,13 @@ namespace exh {
 constexpr int G_DEFAULT = 10;        // inner (unrolled) bits
 constexpr int OS_EXH_VARIANT_ADD_MIN = 1;  // three-input add + min (ALU pipe)
 constexpr int OS_EXH_VARIANT_FUSED = 2;    // FMA-pipe multiply-add + fused add-min
-constexpr int OS_EXH_VARIANT_PACKED = 3;   // two states per add in 16-bit halves, register sub-walk
+constexpr int OS_EXH_VARIANT_PACKED = 3;   // two states per three-input add in 16-bit halves
 constexpr int OS_EXH_VARIANT_DEFAULT = OS_EXH_VARIANT_FUSED;
 // Packed variant: each half holds energy + PACK_BIAS in [0, 32767]; safe when
 // the coefficient magnitudes (upper triangle) sum to at most PACK_MAX_ABS, so
 // that every energy and every coupling sum stays within 16383.
 constexpr int PACK_BIAS = 16384;
 constexpr double PACK_MAX_ABS = 8000.0;
-constexpr int SUB_BITS = 4;          // packed variant: inner bits walked against registers
 constexpr int G_MAX = 10;
 constexpr int INNER_MAX = 1 << G_MAX;
 constexpr int LCAP = 4;              // states kept per thread
@@ -64,12 +63,7 @@ struct Summary {
 template <class T> struct GrayParams {
   T kf[INNER_MAX];                // inner step constants (kf[0] unused)
   T ks[INNER_MAX];                // prefix sums ks[t] = kf[1] + ... + kf[t]
-  // Packed variant (both halves, i.e. times 65537): step t flipping a sub
-  // bit k < SUB_BITS adds kp[t] = +/-(Q_kk + couplings to the set sub bits);
-  // a step flipping k >= SUB_BITS adds kp[t] = kf[t] and moves the sub bits'
-  // outside couplings by qs[t / 2^SUB_BITS][i] = +/- Q_ki.
-  int kp[INNER_MAX];
-  int qs[INNER_MAX >> SUB_BITS][SUB_BITS];
+  int kp[INNER_MAX];              // kf[t] in both 16-bit halves (packed variant)
   T one;                          // 1, as a runtime value
   const T *q;                     // n x n symmetric coefficients
   const T *kf_g;                  // global copy of kf (slow path)
@@ -122,36 +116,30 @@ __device__ __forceinline__ void inner_step(T &E, T &m, const T (&c)[G], const Gr
   }
 }
 
-// MODE 2: one block of 2^G inner states for two walks at once. E, c and cs
+// MODE 2: one block of 2^G inner states for two walks at once. E and c
 // hold two values as x_b * 65536 + x_a, both energies biased into
 // [0, 32767], so plain 32-bit adds update both halves exactly (a packed sum
 // is a sum of packed values) and the per-half minimum is one 16x2
-// instruction. The low SUB_BITS inner bits are walked against cs[], their
-// couplings to every set bit outside them, kept in registers and moved at the
-// steps that flip a higher bit; every state then costs one three-input add
-// whose constant comes from the parameter bank, and every two states one
-// three-input per-half minimum.
+// instruction. Every step is the MODE 0 update on both walks,
+// E += kf[t] +/- c[k], one three-input add whose constant (kf[t] in both
+// halves) comes from the parameter bank; every two steps (four states) one
+// three-input per-half minimum. Both run on the ALU pipe, 0.75 instructions
+// per state. (Constant-bank operands are what decide this form: the 16-bit
+// fused add-min and the multiply-add cannot take one without a separate
+// constant load per step.)
 template <int G, int t>
-__device__ __forceinline__ void packed_step(int &E, int (&cs)[SUB_BITS], const int (&c)[G],
-                                            const GrayParams<int> &P) {
+__device__ __forceinline__ void packed_step(int &E, const int (&c)[G], const GrayParams<int> &P) {
   constexpr int k = ctz_c(t);
   constexpr bool up = (gray_c(t) >> k) & 1;
-  if constexpr (k < SUB_BITS) {
-    E = E + P.kp[t] + (up ? cs[k] : -cs[k]);
-  } else {
-    E = E + P.kp[t] + (up ? c[k] : -c[k]);
-#pragma unroll
-    for (int i = 0; i < SUB_BITS; ++i) cs[i] += P.qs[t >> SUB_BITS][i];
-  }
+  E = E + P.kp[t] + (up ? c[k] : -c[k]);
 }
 
 template <int G, int t>
-__device__ __forceinline__ void packed_pair(int &E, int &m, int (&cs)[SUB_BITS], const int (&c)[G],
-                                            const GrayParams<int> &P) {
-  packed_step<G, t>(E, cs, c, P);
+__device__ __forceinline__ void packed_pair(int &E, int &m, const int (&c)[G], const GrayParams<int> &P) {
+  packed_step<G, t>(E, c, P);
   if constexpr (t + 1 < (1 << G)) {
     const int e1 = E;
-    packed_step<G, t + 1>(E, cs, c, P);
+    packed_step<G, t + 1>(E, c, P);
     m = (int)__vimin3_s16x2((unsigned)m, (unsigned)e1, (unsigned)E);
   } else {
     m = (int)__vimin3_s16x2((unsigned)m, (unsigned)E, (unsigned)E);
@@ -159,20 +147,17 @@ __device__ __forceinline__ void packed_pair(int &E, int &m, int (&cs)[SUB_BITS],
 }
 
 template <int G, int... Is>
-__device__ __forceinline__ void packed_block_impl(int &E, int &m, int (&cs)[SUB_BITS], const int (&c)[G],
-                                                  const GrayParams<int> &P, std::integer_sequence<int, Is...>) {
-  (packed_pair<G, 2 * Is + 1>(E, m, cs, c, P), ...);
+__device__ __forceinline__ void packed_block_impl(int &E, int &m, const int (&c)[G], const GrayParams<int> &P,
+                                                  std::integer_sequence<int, Is...>) {
+  (packed_pair<G, 2 * Is + 1>(E, m, c, P), ...);
 }
 
 // Minimum (per half) over the block that starts at packed energy E with
 // packed outer couplings c.
 template <int G>
 __device__ __forceinline__ int inner_block_packed(int E, const int (&c)[G], const GrayParams<int> &P) {
-  int cs[SUB_BITS];
-#pragma unroll
-  for (int i = 0; i < SUB_BITS; ++i) cs[i] = c[i];
   int m = E;
-  packed_block_impl<G>(E, m, cs, c, P, std::make_integer_sequence<int, (1 << (G - 1))>{});
+  packed_block_impl<G>(E, m, c, P, std::make_integer_sequence<int, (1 << (G - 1))>{});
   return m;
 }
 

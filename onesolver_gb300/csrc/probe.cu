@@ -61,9 +61,10 @@ __global__ void __launch_bounds__(256) int32_probe_kernel(const __grid_constant_
 
 // The per-state instructions of exhaustive variant V (1: three-input add +
 // min; 2: multiply-add + fused add-min; 3: packed 16-bit halves, one
-// three-input add per two states and one three-input per-half min per four),
-// STEPS steps of CHAINS independent chains per thread; the step constants
-// come from the parameter bank as in the enumeration kernel.
+// three-input add per two states and one three-input per-half min per four:
+// the packed walk's whole inner loop), STEPS steps of CHAINS independent
+// chains per thread; the step constants come from the parameter bank as in
+// the enumeration kernel.
 struct PairParams {
   int k[STEPS];
   int k2s[STEPS];

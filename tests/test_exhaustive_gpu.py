@@ -7,6 +7,8 @@ is compared with the oracle's exact-equality set.
 """
 from __future__ import annotations
 
+from pathlib import Path
+
 import numpy as np
 import pytest
 
@@ -136,18 +138,26 @@ def test_invalid_arguments(native, ctx):
         native.exhaustive(f, ctx=ctx)
 
 
-def test_n36_config(native, orc, ctx):
-    """Dense N=36, integer coefficients in [-8, 8] (2^36 states)."""
-    f = random_int_qubo(36, 0)
-    res = native.exhaustive(f, ctx=ctx)
+@pytest.mark.parametrize("seed", [0, 1, 2])
+def test_n36_config(native, orc, ctx, seed):
+    """Dense N=36, integer coefficients in [-8, 8] (2^36 states): the ground
+    energy, the reference's answer, the number of minimisers and every
+    minimiser equal the oracle's own full scan of all 2^36 states, committed
+    as tests/golden/exhaustive36_golden.json (made by
+    tests/golden/make_exhaustive36.py)."""
+    import json
+    gold = json.loads((Path(__file__).parent / "golden" / "exhaustive36_golden.json").read_text())[str(seed)]
+    f = random_int_qubo(36, seed)
+    res = native.exhaustive(f, ctx=ctx, max_minimisers=1 << 16)
     assert res.states_enumerated == 1 << 36
-    # Size-independent properties: the minimisers have the reported energy
-    # under the reference's energy function, and they are sorted and unique.
-    assert res.count >= 1
-    for s in res.states.tolist():
-        assert orc.energy_bits(f, s) == res.energy
-    assert res.state == int(res.states[0])
-    assert np.all(np.diff(res.states.astype(np.int64)) > 0)
+    assert res.energy == gold["energy"]
+    assert res.state == gold["state"]
+    assert res.count == gold["count"]
+    assert res.states.tolist() == gold["states"]
+    # The fused variant reaches the same answer.
+    r2 = native.exhaustive(f, ctx=ctx, max_minimisers=1 << 16, variant=2)
+    assert (r2.energy, r2.state, r2.count, r2.states.tolist()) == (res.energy, res.state, res.count,
+                                                                  gold["states"])
     # Shards of 2^22 states agree with the oracle's scan of the same range,
     # and no shard goes below the global minimum.
     for p in (0, (1 << 14) - 1, 5461, int(res.state >> 22)):
@@ -161,10 +171,42 @@ def test_n36_config(native, orc, ctx):
 def test_inner_widths_agree(native, orc, ctx, n):
     f = random_int_qubo(n, 40 + n, -2, 2)
     res = [native.exhaustive(f, ctx=ctx, inner_bits=g, variant=v, max_minimisers=1 << 16)
-           for g in (9, 10) for v in (1, 2)]
+           for g in (9, 10) for v in (1, 2, 3)]
     for r in res[1:]:
         assert (r.energy, r.state, r.count, r.states.tolist()) == \
             (res[0].energy, res[0].state, res[0].count, res[0].states.tolist())
-    if n <= 21:
-        e, count, states = orc.exhaustive_all(f)
-        assert res[0].energy == e and res[0].count == count
+    # Every width and variant against the oracle's full scan.
+    e, count, states = orc.exhaustive_all(f) if n <= 21 else orc.exhaustive_int_all(f)
+    assert (res[0].energy, res[0].count) == (e, count)
+    assert res[0].state == int(states[0])
+    assert res[0].states.tolist() == states.tolist()
+
+
+@pytest.mark.parametrize("fill", ["neg", "pos", "alternating"])
+def test_packed_variant_at_its_range_limit(native, orc, ctx, fill):
+    """The packed variant holds energies in 16-bit halves; it is exact up to
+    coefficient magnitudes summing to 8,000 (here 7,980, all of one sign, so
+    the extreme energies and coupling sums reach the limit)."""
+    n = 20
+    v = {"neg": -38.0, "pos": 38.0}.get(fill)
+    if v is None:
+        f = np.where((np.arange(n)[:, None] + np.arange(n)[None, :]) % 2 == 0, 38.0, -38.0)
+    else:
+        f = np.full((n, n), v)
+    assert np.abs(np.triu(f)).sum() == 7980
+    plan = native.ExhaustivePlan(f, ctx=ctx, max_minimisers=1 << 16)
+    assert plan.variant == 3
+    plan.close()
+    for variant in (0, 2, 3):
+        check_against_oracle(native, orc, ctx, f, variant=variant)
+
+
+def test_packed_variant_only_where_exact(native, ctx):
+    f = np.full((20, 20), 40.0)   # magnitudes sum to 8,400
+    plan = native.ExhaustivePlan(f, ctx=ctx)
+    assert plan.variant == 2      # the default falls back to the 32-bit pair
+    plan.close()
+    with pytest.raises(native.OneSolverError, match="packed"):
+        native.exhaustive(f, ctx=ctx, variant=3)
+    with pytest.raises(native.OneSolverError):
+        native.exhaustive(random_int_qubo(20, 0), ctx=ctx, variant=4)

@@ -145,3 +145,43 @@ def test_exhaustive_all_counts_ties(orc):
 def test_read_maps_first_key_wins():
     n, lin, quad = read_maps("p qubo 0 3 1 1\n0 0 1\n0 0 5\n0 2 3\n")
     assert n == 3 and lin == {0: 1.0} and quad == {(0, 2): 3.0}
+
+
+@pytest.mark.parametrize("n,seed,lo,hi", [(1, 0, -8, 8), (9, 5, 0, 0), (12, 1, -8, 8), (16, 4, -1, 1),
+                                          (18, 2, -8, 8), (20, 3, -2, 2)])
+def test_integer_table_scan_matches_reference_loop(orc, n, seed, lo, hi):
+    """The byte-table scan that makes the n = 36 fixtures equals the
+    reference's O(n^2)-per-state FP64 loop (energy, count, every minimiser)."""
+    f = random_int_qubo(n, seed, lo, hi)
+    e, count, states = orc.exhaustive_all(f)
+    ei, ci, si = orc.exhaustive_int_all(f)
+    assert (ei, ci) == (e, count)
+    assert si.tolist() == states.tolist()
+    # a sub-range, as shards use it
+    if n >= 12:
+        lo_s, hi_s = 3 << (n - 4), 7 << (n - 4)
+        e2, c2, s2 = orc.exhaustive_all(f, lo_s, hi_s)
+        assert orc.exhaustive_int_all(f, lo_s, hi_s)[:2] == (e2, c2)
+
+
+def test_integer_table_scan_rejects_fractions(orc):
+    f = random_int_qubo(8, 0)
+    f[2, 5] = f[5, 2] = 0.5
+    with pytest.raises(ValueError):
+        orc.exhaustive_int_all(f)
+
+
+def test_exhaustive36_fixture_is_consistent(orc):
+    """The committed n = 36 answers: each listed minimiser has the listed
+    energy under the reference's FP64 energy function, the list is sorted,
+    and its first entry is the reference's answer."""
+    import json
+    from pathlib import Path
+    data = json.loads((Path(__file__).parent / "golden" / "exhaustive36_golden.json").read_text())
+    assert sorted(data) == ["0", "1", "2"]
+    for seed, d in data.items():
+        f = random_int_qubo(36, int(seed))
+        assert d["count"] == len(d["states"]) >= 1
+        assert d["states"] == sorted(d["states"]) and d["state"] == d["states"][0]
+        for s in d["states"]:
+            assert orc.energy_bits(f, s) == d["energy"]
