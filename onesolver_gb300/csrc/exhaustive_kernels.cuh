@@ -408,6 +408,12 @@ __device__ __forceinline__ void process_item(unsigned long long item, const Gray
 // (x_b * 65536 + x_a; c_b = c_a + Q[top][.]). A block pair whose smaller
 // half-minimum reaches the bound is walked again state by state, each half
 // that reaches it on its own, exactly as MODE 1 does.
+//
+// Between block pairs one of the W = loop_bits - 1 walked bits G + w flips.
+// Its energy delta splits into bw[w] (its diagonal and its couplings to the
+// item's fixed set bits, summed once per item in the pass that builds the
+// coupling vector) plus its couplings to the other walked bits that are set
+// (at most three loads), instead of a row sum over every set bit per flip.
 template <int G>
 __device__ __forceinline__ void process_item_packed(unsigned long long item, const GrayParams<int> &P,
                                                     ThreadBest<int> &tb, CollectState &cs) {
@@ -417,10 +423,14 @@ __device__ __forceinline__ void process_item_packed(unsigned long long item, con
   const int *__restrict__ rowt = q + (size_t)top * n;
   unsigned long long xa = P.prefix_state | (item << (G + P.loop_bits));
   const int Ea = energy_from_scratch(q, n, xa);
+  const int W = P.loop_bits - 1;  // walked bits G .. G + W - 1 (W <= LOOP_BITS - 1 = 4)
   int ca[G];
 #pragma unroll
   for (int i = 0; i < G; ++i) ca[i] = 0;
   int sumt = rowt[top];
+  int bw[LOOP_BITS - 1];
+#pragma unroll
+  for (int w = 0; w < LOOP_BITS - 1; ++w) bw[w] = w < W ? q[(size_t)(G + w) * n + G + w] : 0;
   {
     unsigned long long r = xa;
     while (r) {
@@ -429,6 +439,9 @@ __device__ __forceinline__ void process_item_packed(unsigned long long item, con
       const int *row = q + (size_t)j * n;
 #pragma unroll
       for (int i = 0; i < G; ++i) ca[i] += row[i];
+#pragma unroll
+      for (int w = 0; w < LOOP_BITS - 1; ++w)
+        if (w < W) bw[w] += row[G + w];
       sumt += rowt[j];
     }
   }
@@ -471,16 +484,17 @@ __device__ __forceinline__ void process_item_packed(unsigned long long item, con
       }
     }
     if (B + 1 < npairs) {
-      const int mbit = G + __ffs((int)(B + 1)) - 1;
+      const int w = __ffs((int)(B + 1)) - 1;
+      const int mbit = G + w;
       const unsigned long long bm = 1ull << mbit;
       const bool was = (xa & bm) != 0;
       const int *row = q + (size_t)mbit * n;
-      int sum = row[mbit];
-      unsigned long long r = xa & ~bm;
-      while (r) {
-        const int j = __ffsll((long long)r) - 1;
-        r &= r - 1;
-        sum += row[j];
+      const unsigned walked = (unsigned)(xa >> G) & ((1u << W) - 1u) & ~(1u << w);
+      int sum = 0;
+#pragma unroll
+      for (int v = 0; v < LOOP_BITS - 1; ++v) {
+        if (v == w) sum += bw[v];
+        if ((walked >> v) & 1u) sum += row[G + v];
       }
       const int sum2 = sum * 65537 + row[top] * 65536;  // half b also has `top` set
       E2s += was ? -sum2 : sum2;
@@ -535,7 +549,7 @@ __device__ __forceinline__ void cta_reduce(const GrayParams<T> &P, ThreadBest<T>
 }
 
 template <class T, int G, bool COLLECT, int MODE = 0>
-__global__ void __launch_bounds__(THREADS) gray_kernel(const __grid_constant__ GrayParams<T> P) {
+__global__ void __launch_bounds__(THREADS, sizeof(T) == 4 ? 5 : 1) gray_kernel(const __grid_constant__ GrayParams<T> P) {
   ThreadBest<T> tb;
   tb.best = tmax<T>();
   tb.cnt = 0;
