@@ -415,7 +415,7 @@ def bench_sa(args, ctx, pg, rank, world, workload):
     t_step = max_over_ranks(pg, statistics.mean(step_ms))
     value = world * attempts / (t_step * 1e-3)
     e2e_t = []
-    for _ in range(max(2, steps // 5)):
+    for _ in range(max(1 if workload == "sa-batch" else 2, steps // 5)):
         t0 = time.perf_counter()
         r = upload()
         e2e_t.append(time.perf_counter() - t0)
@@ -434,6 +434,23 @@ def bench_sa(args, ctx, pg, rank, world, workload):
     acc_rate = res.accepted / max(res.attempts, 1)
     # The result counters cover the last executed step.
     achieved = smem_bytes / (k_ms * 1e-3) / 1e9
+    roofline = {"bound": "smem", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "peak_source": "os_probe_smem_row_peak (128-bit shared loads + paired FP32 FMAs) measured in this "
+                               "run"}
+    if workload == "sa-chimera":
+        # The sparse sweep is issue-bound: its roofline is issue-slot use,
+        # warp instructions per attempt (ncu, SPARSE_WARP_INST_PER_ATTEMPT)
+        # times attempts/s over one warp instruction per scheduler per clock.
+        sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+        mhz = (clocks or {}).get("sm_mhz") or load_peaks().get("sm_max_mhz", 2070.0)
+        issue = attempts / (k_ms * 1e-3) * SPARSE_WARP_INST_PER_ATTEMPT
+        issue_peak = sms * 4 * mhz * 1e6
+        roofline = {"bound": "issue", "achieved": issue, "peak": issue_peak, "unit": "warp-inst/s",
+                    "frac": issue / issue_peak, "warp_inst_per_attempt": SPARSE_WARP_INST_PER_ATTEMPT,
+                    "thread_inst_per_attempt": SPARSE_WARP_INST_PER_ATTEMPT * SPARSE_LANES_PER_INST,
+                    "smem_view": {"achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak},
+                    "peak_source": "SMs x 4 schedulers x median SM clock; instructions per attempt from "
+                                   "profiles/sa_sparse_chimera2048.md"}
     out = {
         "metric": "SA spin-flip attempts/s",
         "value": value, "unit": "attempts/s", "ms_per_step": t_step, "dtype": "fp32",
@@ -441,16 +458,13 @@ def bench_sa(args, ctx, pg, rank, world, workload):
                    "l2": "flushed (256 MB write) before every timed step",
                    "parallelism": f"replicas x{world}" if world > 1 else "1 GPU"},
         "result": {"best_energy": res.energy, "acceptance_rate": acc_rate, "max_field_drift": res.max_field_drift},
-        "roofline": {"bound": "smem", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": TRAFFIC.get(workload), "kernel_ms": k_ms,
+        "roofline": {**roofline, "traffic": TRAFFIC.get(workload), "kernel_ms": k_ms,
                      "kernel_attempts_per_s": attempts / (k_ms * 1e-3),
                      "bytes_per_step": smem_bytes,
                      "fp32_fma_view": None if fmas_per_step is None else {
                          "achieved_gflops": 2 * fmas_per_step / (k_ms * 1e-3) / 1e9, "peak_gflops": fma_peak,
                          "frac": 2 * fmas_per_step / (k_ms * 1e-3) / 1e9 / fma_peak,
-                         "note": "n FP32 FMAs per attempt over os_probe_fp32_fma_peak"},
-                     "peak_source": "os_probe_smem_row_peak (128-bit shared loads + paired FP32 FMAs) "
-                                    "measured in this run"},
+                         "note": "n FP32 FMAs per attempt over os_probe_fp32_fma_peak"}},
         "e2e": {"value": world * attempts / e2e_step, "unit": "attempts/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(n * T + 8 * T + 8 * 3), "ms_per_step": e2e_step * 1e3},
         "gpu_launches": int(sum(launches)),
@@ -658,11 +672,20 @@ def bench_learned(args, ctx, pg, rank, world):
 
 # DRAM bytes (read + write) per launch of the dominant kernel, from one ncu
 # capture (dram__bytes_read.sum + dram__bytes_write.sum) of the n = 36
-# launch. The exhaustive launch moves a constant 2.03 MB (coefficients,
-# per-CTA records and kept states) whatever the number of states. The SA kernels keep their
-# working set on chip for a launch; their DRAM bytes per launch depend on the
-# chunk length, not on the attempts, and are not reported.
-TRAFFIC: dict = {"exhaustive36": 2029056}
+# launch (profiles/exhaustive_gray_n36.md): a constant ~64 KB (coefficients
+# and parameters; the per-CTA records stay in L2) whatever the number of
+# states. The SA kernels keep their working set on chip for a launch; their
+# DRAM bytes per launch depend on the chunk length, not on the attempts, and
+# are not reported.
+TRAFFIC: dict = {"exhaustive36": 63488}
+
+# Warp instructions per attempt of the sparse sweep kernel and the active
+# lanes per instruction, from one ncu capture of the Chimera 2048 profile
+# case (smsp__inst_executed.sum over 1,024 trajectories x 50 sweeps x 2,048
+# sites; smsp__thread_inst_executed_per_inst_executed.ratio), summarised in
+# profiles/sa_sparse_chimera2048.md.
+SPARSE_WARP_INST_PER_ATTEMPT = 540055768 / (1024 * 50 * 2048)
+SPARSE_LANES_PER_INST = 29.90
 
 
 # ---------------------------------------------------------------------------
@@ -904,15 +927,26 @@ def main():
         out = bench_sa(args, ctx, pg, rank, world, args.workload)
 
     if args.secondary and args.workload == "exhaustive36":
+        # The SA configurations beside the headline: Chimera (config 3), SK
+        # n = 1024 (the learned warm start's family) and the batched
+        # configuration (config 4; 14 s per step, so one warm-up and one timed
+        # step), each with its CPU baseline (the reference's algorithm on the
+        # host cores, a bounded sample of the same workload).
         sec = {}
-        for w, k in (("sa-chimera", 3), ("sa-sk", 3)):
+        for w, k, wu in (("sa-chimera", 3, 3), ("sa-sk", 3, 3), ("sa-batch", 1, 1)):
             a2 = argparse.Namespace(**vars(args))
-            a2.steps, a2.warmup = k, 3
+            a2.steps, a2.warmup = k, wu
             r = bench_sa(a2, ctx, pg, rank, world, w)
             sec[w] = {"value": r["value"], "unit": r["unit"], "config": r["config"]["workload"],
+                      "steps": k, "warmup": wu, "ms_per_step": r["ms_per_step"],
                       "kernel_attempts_per_s": r["roofline"]["kernel_attempts_per_s"],
                       "roofline": {k2: r["roofline"][k2] for k2 in ("bound", "achieved", "peak", "unit", "frac")},
                       "e2e": r["e2e"]["value"], "result": r["result"], "gpu_launches": r["gpu_launches"]}
+            if rank == 0 and world == 1 and args.cpu_baseline:
+                threads = os.cpu_count() or 1
+                rate, desc, dt = cpu_sa_rate(w, 5.0, threads)
+                sec[w]["cpu_baseline"] = {"value": rate, "unit": "attempts/s", "cores": threads, "kind": "port",
+                                          "sample": desc + f" ({dt:.1f} s), full FP64 energy per attempt"}
         out["secondary"] = sec
 
     if rank == 0 and world == 1 and args.cpu_baseline and args.workload not in ("sa-learned", "pt-droplet", "pa-droplet"):
