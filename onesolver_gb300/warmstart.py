@@ -13,20 +13,47 @@ the C ABI):
 5. ``time_to_target`` -- the sweep budget (and wall time) each method needs to
    come within a relative gap of a target energy.
 
+``load_shipped`` returns the network the library ships for SK n = 1024
+(trained by ``python -m onesolver_gb300.train_warmstart`` on 4,096 instances)
+with its held-out seeds and their 10^5-sweep plain-SA targets.
+
 Plain random-init SA is both the fallback and the yardstick: targets come from
 long plain runs and every comparison uses the same number of trajectories.
 """
 from __future__ import annotations
 
+import json
 import math
 import time
 from dataclasses import dataclass, field
+from pathlib import Path
 from typing import Optional, Sequence
 
 import numpy as np
 
 from . import (ACCEPT_PHYSICAL, BatchedAnnealPlan, Context, WarmStartNet, anneal, default_context,
                geometric_schedule)
+
+
+SHIPPED = Path(__file__).resolve().parent / "data" / "warmstart_sk1024.npz"
+
+
+@dataclass
+class Shipped:
+    """The network the library ships for SK n = 1024 (train_warmstart.py) and
+    its held-out seeds with their 10^5-sweep plain-SA target energies."""
+    net: "WarmStartNet"
+    meta: dict
+    eval_seeds: np.ndarray
+    targets: np.ndarray
+
+
+def load_shipped(ctx: Optional[Context] = None) -> Shipped:
+    d = np.load(SHIPPED)
+    meta = json.loads(str(d["meta"]))
+    net = WarmStartNet(hidden=meta["hidden"], layers=meta["layers"], orient=meta["orient"], ctx=ctx)
+    net.set_params(d["params"])
+    return Shipped(net, meta, d["eval_seeds"].copy(), d["targets"].copy())
 
 
 def sk_qubo(n: int, seed: int) -> np.ndarray:
