@@ -617,10 +617,11 @@ def bench_learned(args, ctx, pg, rank, world):
         t_gate = time.perf_counter() - t0
         plain = ws.time_to_target(f, target, ctx=ctx)                       # config schedule, fair coins
         cold = ws.time_to_target(f, target, beta_min=WARM_BETA_MIN, ctx=ctx)  # warm runs' schedule, fair coins
-        warm = ws.time_to_target(f, target, init_prob=ws.sharpen(prob, gate.temperature), beta_min=WARM_BETA_MIN,
-                                 ctx=ctx)
-        # The warm arm pays for its prediction; the gate's probe runs are reported apart.
-        warm_s = warm.seconds + t_pred if warm.seconds is not None else None
+        # The warm arm predicts on the device from each try's own plan
+        # (os_sa_plan_warm_start), inside its timed region; the host-path
+        # prediction above (predict_s) and the gate's probe runs are reported apart.
+        warm = ws.time_to_target(f, target, net=net, beta_min=WARM_BETA_MIN, ctx=ctx)
+        warm_s = warm.seconds
         chosen_s = warm_s if gate.use_warm else cold.seconds
         chosen_sw = warm.sweeps if gate.use_warm else cold.sweeps
         rows.append({"seed": seed, "target": target, "use_warm": bool(gate.use_warm),
@@ -645,7 +646,7 @@ def bench_learned(args, ctx, pg, rank, world):
     value = med("chosen_s", both)
     out = {
         "metric": "SA time-to-target (within 0.5% of a 10^5-sweep plain-SA best), learned warm start with probe "
-                  "gate (prediction time included, probe runs reported apart)",
+                  "gate (device-side prediction inside each timed run, probe runs reported apart)",
         "value": value, "unit": "s", "ms_per_step": None, "dtype": "fp32 fields, bf16 network",
         "higher_is_better": False,
         "config": {"workload": f"SK n=1024 J~N(0,1/n); network trained on {meta['train_seeds'][1]} instances "

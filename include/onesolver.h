@@ -568,8 +568,9 @@ os_status os_philox_sample(os_ctx *ctx, const uint32_t ctr[4],
  * probabilities P(x_i = 1) for os_sa_params.init_prob. The reference always
  * starts from fair coins (annealing.hpp:91-93); plain random-init annealing
  * stays the fallback. Hidden width 64 (the kernels are built for it), 1..8
- * layers; BF16 tensor-core (mma.sync) products with FP32 accumulation for
- * the coupling-matrix messages, FP32 elsewhere; Adam on the GPU. With
+ * layers; BF16 products on the 5th-generation tensor cores (tcgen05.mma, FP32
+ * accumulator in tensor memory) for the coupling-matrix messages, FP32
+ * elsewhere; Adam on the GPU. With
  * orient = 1 labels are oriented so that spin 0 is 1 and predictions come
  * in that orientation (for field-free Ising QUBOs, which are symmetric under
  * the global flip); orient = 0 keeps labels as given. */
@@ -590,6 +591,13 @@ os_status os_mpnn_loss_grad(os_mpnn *model, int32_t index, float *loss, float *g
 os_status os_mpnn_train(os_mpnn *model, int32_t epochs, float lr, uint64_t shuffle_seed, float *epoch_loss);
 /* Per-spin P(x_i = 1) (n floats) for a new instance. */
 os_status os_mpnn_predict(os_mpnn *model, const os_qubo_dense *qubo, float *prob);
+/* The same prediction for a dense annealing plan's own instance, from the
+ * matrix the plan already holds on the device, written straight into the
+ * plan's initial-spin probabilities (as if os_sa_params.init_prob had been
+ * given): no host copy either way and no synchronisation; it only enqueues
+ * on the shared context's stream, before the plan's next execute. The plan
+ * and the network must share a context. */
+os_status os_sa_plan_warm_start(os_sa_plan *plan, os_mpnn *model);
 
 /* Measured roofline denominators for the integer/FP32/shared-memory-bound
  * paths (the measured peaks cover HBM copy bandwidth and bf16 GEMMs

@@ -198,6 +198,7 @@ SIGNATURES = {
     "os_mpnn_loss_grad": (C.c_int, [_P, C.c_int32, C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_size_t]),
     "os_mpnn_train": (C.c_int, [_P, C.c_int32, C.c_float, C.c_uint64, C.POINTER(C.c_float)]),
     "os_mpnn_predict": (C.c_int, [_P, C.POINTER(_QuboDense), C.POINTER(C.c_float)]),
+    "os_sa_plan_warm_start": (C.c_int, [_P, _P]),
     "os_probe_int32_peak": (C.c_int, [_P, C.POINTER(C.c_double)]),
     "os_probe_exhaustive_pair": (C.c_int, [_P, C.c_int32, C.POINTER(C.c_double)]),
     "os_probe_fp32_fma_peak": (C.c_int, [_P, C.POINTER(C.c_double)]),
@@ -749,6 +750,11 @@ class AnnealPlan(_PlanReplay):
 
     def _sizes(self) -> list:
         return [self.n]
+
+    def warm_start(self, net: "WarmStartNet") -> None:
+        """Initial spins from the network's prediction on this plan's own
+        (device-resident) matrix, for the next executes (dense plans)."""
+        _check(lib().os_sa_plan_warm_start(self._h, net._h))
 
     def close(self) -> None:
         if self._h:

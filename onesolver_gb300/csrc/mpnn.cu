@@ -26,9 +26,10 @@
 // tie), and the prediction is in that orientation. General QUBOs keep their
 // labels as given.
 //
-// The (n x n) x (n x H) products run on the tensor cores with mma.sync
-// m16n8k16 BF16 -> FP32; the small (n x H) x (H x H) products, the weight
-// gradients and the element-wise parts run on FP32 CUDA cores.
+// The (n x n) x (n x H) products run on the 5th-generation tensor cores
+// (tcgen05.mma kind::f16, BF16 x BF16 -> FP32 in tensor memory); the small
+// (n x H) x (H x H) products, the weight gradients and the element-wise parts
+// run on FP32 CUDA cores.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -39,6 +40,8 @@
 
 #include "common.cuh"
 #include "philox.cuh"
+#include "sa_plan.cuh"
+#include "tc05.cuh"
 
 namespace os {
 namespace mpnn {
@@ -48,85 +51,116 @@ constexpr int SPEC_RHO_ITERS = 16;   // power iterations on C^ for its spectral 
 constexpr int SPEC_ITERS = 96;       // power iterations on (sigma I - C^), sigma = 1.05 rho
 
 // ---------------------------------------------------------------------------
-// C^ (n x n, BF16, row-major) times Hb (n x H, BF16, row-major) -> out
-// (n x H, FP32). CTA: 64 rows x 64 columns, 4 warps of 16 rows, K step 32.
+// C^ (np x np, BF16, row-major) times Hb (np x 64, BF16), on the
+// 5th-generation tensor cores: out (np x 64, FP32, row-major).
+//
+// Hb is passed transposed (HbT, 64 x np), so both operands are K-major. A CTA
+// computes 128 rows x 64 columns over one K range of `ks` (split K: CTA
+// (x, y) covers rows [128 x, 128 x + 128) and K [y ks, (y + 1) ks), and writes
+// its partial product to out + y * np * 64). K advances in chunks of 64: the
+// 4 warps stage the chunk's A (128 x 64) and B (64 x 64) tiles into one of
+// two shared-memory buffers as 8-row x 16-byte core matrices (tc05.cuh), one
+// elected thread issues four K = 16 tcgen05.mma (kind::f16, BF16 x BF16 ->
+// FP32) into a 128 x 64 accumulator in 64 TMEM columns and commits them to
+// the buffer's mbarrier, which frees it for the chunk after next. The
+// epilogue reads the accumulator with tcgen05.ld (warp w: rows 32 w ..
+// 32 w + 31). Rows past np are staged as zeros and not stored. Every wait is
+// bounded; on a wait running out the CTA stops, frees its TMEM and sets
+// *status.
 // ---------------------------------------------------------------------------
-constexpr int GM = 64, GN = 64, GK = 32;
+constexpr int GN = 64;                                   // hidden width the kernels are built for
+constexpr int TM = 128, TK = 64;
+constexpr int TC_STAGE_A = TM * TK * 2, TC_STAGE_B = GN * TK * 2;
+constexpr int TC_SMEM = 2 * (TC_STAGE_A + TC_STAGE_B);   // 48 KB
+constexpr uint32_t TC_WAIT_LIMIT = 1u << 26;
 
-__device__ __forceinline__ void mma_bf16_16816(float (&d)[4], const uint32_t (&a)[4], const uint32_t (&b)[2]) {
-  asm volatile(
-      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-      "{%0,%1,%2,%3};\n"
-      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
-      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
-}
-
-__device__ __forceinline__ uint32_t pack2(__nv_bfloat16 lo, __nv_bfloat16 hi) {
-  uint32_t r;
-  r = (uint32_t)__bfloat16_as_ushort(lo) | ((uint32_t)__bfloat16_as_ushort(hi) << 16);
-  return r;
-}
-
-// Requires n % 32 == 0 (padded) and H == 64. Split K: CTA (x, y) covers rows
-// [64 x, 64 x + 64) and K range [y ks, (y + 1) ks) and writes its partial
-// product to out + y * n * 64 (ks % 32 == 0).
-__global__ void __launch_bounds__(128) gemm_ch_kernel(const __nv_bfloat16 *__restrict__ A, int n, int ks,
-                                                      const __nv_bfloat16 *__restrict__ B, float *__restrict__ out) {
-  __shared__ __nv_bfloat16 sA[GM][GK + 8];
-  __shared__ __nv_bfloat16 sB[GK][GN + 8];
-  const int row0 = blockIdx.x * GM;
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int g = lane >> 2, tg = lane & 3;
-  float acc[GN / 8][4];
-#pragma unroll
-  for (int j = 0; j < GN / 8; ++j)
-#pragma unroll
-    for (int e = 0; e < 4; ++e) acc[j][e] = 0.f;
-  out += (size_t)blockIdx.y * n * GN;
-  const int kb = blockIdx.y * ks;
-  for (int k0 = kb; k0 < kb + ks; k0 += GK) {
-    // Stage A (64 x 32) and B (32 x 64): 2048 elements each, 16 per thread.
-    for (int i = threadIdx.x; i < GM * GK; i += blockDim.x) {
-      const int r = i / GK, c = i % GK;
-      const int gr = row0 + r;
-      sA[r][c] = gr < n ? A[(size_t)gr * n + k0 + c] : __float2bfloat16(0.f);
-    }
-    for (int i = threadIdx.x; i < GK * GN; i += blockDim.x) {
-      const int r = i / GN, c = i % GN;
-      sB[r][c] = B[(size_t)(k0 + r) * GN + c];
-    }
-    __syncthreads();
-#pragma unroll
-    for (int kk = 0; kk < GK; kk += 16) {
-      uint32_t a[4];
-      const int ar = warp * 16 + g;
-      a[0] = pack2(sA[ar][kk + tg * 2], sA[ar][kk + tg * 2 + 1]);
-      a[1] = pack2(sA[ar + 8][kk + tg * 2], sA[ar + 8][kk + tg * 2 + 1]);
-      a[2] = pack2(sA[ar][kk + tg * 2 + 8], sA[ar][kk + tg * 2 + 9]);
-      a[3] = pack2(sA[ar + 8][kk + tg * 2 + 8], sA[ar + 8][kk + tg * 2 + 9]);
-#pragma unroll
-      for (int j = 0; j < GN / 8; ++j) {
-        uint32_t b[2];
-        const int bc = j * 8 + g;
-        b[0] = pack2(sB[kk + tg * 2][bc], sB[kk + tg * 2 + 1][bc]);
-        b[1] = pack2(sB[kk + tg * 2 + 8][bc], sB[kk + tg * 2 + 9][bc]);
-        mma_bf16_16816(acc[j], a, b);
+__global__ void __launch_bounds__(128) gemm_ch_kernel(const __nv_bfloat16 *__restrict__ A, int np, int ks,
+                                                      const __nv_bfloat16 *__restrict__ BT, float *__restrict__ out,
+                                                      int *__restrict__ status) {
+  extern __shared__ __align__(1024) unsigned char tc_smem[];
+  auto sA = [&](int b) { return tc_smem + b * TC_STAGE_A; };
+  auto sB = [&](int b) { return tc_smem + 2 * TC_STAGE_A + b * TC_STAGE_B; };
+  __shared__ __align__(8) uint64_t bar[2];
+  __shared__ uint32_t tmem_base;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int row0 = blockIdx.x * TM, kb = blockIdx.y * ks;
+  out += (size_t)blockIdx.y * np * GN;
+  if (warp == 0) {
+    tc05::tmem_alloc(&tmem_base, GN);
+    tc05::tmem_relinquish();
+  }
+  if (tid == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    mbar_fence_init();
+  }
+  tc05::fence_before_sync();
+  __syncthreads();
+  tc05::fence_after_sync();
+  const uint32_t tmem = tmem_base;
+  constexpr uint32_t idesc = tc05::idesc_bf16_f32(TM, GN);
+  const int nchunks = ks / TK;
+  bool bad = false;
+  for (int c = 0; c < nchunks; ++c) {
+    const int b = c & 1;
+    if (c >= 2) {  // the MMAs of chunk c - 2 have released buffer b
+      const bool ok = mbar_wait_bounded(&bar[b], (uint32_t)(((c - 2) >> 1) & 1), TC_WAIT_LIMIT);
+      if (__syncthreads_or(!ok)) {
+        bad = true;
+        break;
       }
     }
+    const int k0 = kb + c * TK;
+    for (int p = tid; p < TM * (TK / 8); p += 128) {
+      const int r = p >> 3, kg = p & 7, row = row0 + r;
+      const uint4 v = row < np ? *reinterpret_cast<const uint4 *>(A + (size_t)row * np + k0 + kg * 8)
+                               : make_uint4(0u, 0u, 0u, 0u);
+      *reinterpret_cast<uint4 *>(sA(b) + tc05::core_offset(r, kg)) = v;
+    }
+    for (int p = tid; p < GN * (TK / 8); p += 128) {
+      const int r = p >> 3, kg = p & 7;
+      *reinterpret_cast<uint4 *>(sB(b) + tc05::core_offset(r, kg)) =
+          *reinterpret_cast<const uint4 *>(BT + (size_t)r * np + k0 + kg * 8);
+    }
+    tc05::fence_proxy_async_smem();
     __syncthreads();
-  }
-  const int r_lo = row0 + warp * 16 + g, r_hi = r_lo + 8;
+    if (tid == 0) {
+      tc05::fence_after_sync();
 #pragma unroll
-  for (int j = 0; j < GN / 8; ++j) {
-    const int c = j * 8 + tg * 2;
-    if (r_lo < n) {
-      out[(size_t)r_lo * GN + c] = acc[j][0];
-      out[(size_t)r_lo * GN + c + 1] = acc[j][1];
+      for (int kk = 0; kk < TK / 16; ++kk) {
+        const uint64_t ad = tc05::smem_desc(smem_u32(sA(b)) + kk * 256, 128, 1024);
+        const uint64_t bd = tc05::smem_desc(smem_u32(sB(b)) + kk * 256, 128, 1024);
+        tc05::mma_bf16(tmem, ad, bd, idesc, (c > 0 || kk > 0) ? 1u : 0u);
+      }
+      tc05::commit(&bar[b]);
     }
-    if (r_hi < n) {
-      out[(size_t)r_hi * GN + c] = acc[j][2];
-      out[(size_t)r_hi * GN + c + 1] = acc[j][3];
+  }
+  if (!bad) {  // the last commit covers every MMA issued before it
+    const int c = nchunks - 1;
+    const bool ok = mbar_wait_bounded(&bar[c & 1], (uint32_t)((c >> 1) & 1), TC_WAIT_LIMIT);
+    bad = __syncthreads_or(!ok);
+  }
+  tc05::fence_after_sync();
+  if (!bad) {
+    const int row = row0 + 32 * warp + lane;  // accumulator row = TMEM lane
+#pragma unroll 1
+    for (int c2 = 0; c2 < GN / 32; ++c2) {
+      uint32_t v[32];
+      tc05::ld_32x32b_x32(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)(c2 * 32), v);
+      tc05::wait_ld();
+      if (row < np) {
+#pragma unroll
+        for (int j = 0; j < 32; ++j) out[(size_t)row * GN + c2 * 32 + j] = __uint_as_float(v[j]);
+      }
     }
+  } else if (tid == 0 && status) {
+    atomicExch(status, 1);
+  }
+  tc05::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) {
+    tc05::fence_after_sync();
+    tc05::tmem_dealloc(tmem, GN);
   }
 }
 
@@ -158,9 +192,13 @@ __global__ void linear_kernel(const float *__restrict__ A, const float *__restri
   out[(size_t)i * Hh + h] = relu ? fmaxf(acc, 0.f) : acc;
 }
 
-__global__ void to_bf16_kernel(const float *__restrict__ in, __nv_bfloat16 *__restrict__ out, size_t count) {
+// in (rows x 64, FP32, row-major) -> out (64 x np, BF16): the transposed,
+// K-major operand of gemm_ch_kernel.
+__global__ void to_bf16_t_kernel(const float *__restrict__ in, __nv_bfloat16 *__restrict__ out, int rows, int np) {
   const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < count) out[i] = __float2bfloat16(in[i]);
+  if (i >= (size_t)rows * GN) return;
+  const int r = (int)(i / GN), h = (int)(i % GN);
+  out[(size_t)h * np + r] = __float2bfloat16(in[i]);
 }
 
 // logits, probabilities, loss terms and dlogit for one instance.
@@ -327,7 +365,8 @@ struct os_mpnn {
   // work buffers for n up to cap
   int cap = 0;
   DevBuf<float> X0pre, Hs, pres, M, dH, dZ, dM, prob, dlogit, loss, gpart;
-  DevBuf<__nv_bfloat16> Hb;
+  DevBuf<__nv_bfloat16> Hb;            // the message product's operand, transposed (64 x np)
+  DevBuf<int> tc_status;                // set when a tensor-core kernel's bounded wait ran out
   // prediction: persistent buffers and the captured staging + forward graph
   // (valid for pgraph_n spins while the work buffers keep capacity pgraph_cap)
   std::unique_ptr<MpnnInstance> pin;
@@ -362,19 +401,35 @@ void ensure_work(os_mpnn *m, int np) {
   m->loss.alloc(1);
   m->Hb.alloc(nh);
   m->gpart.alloc(4 * nh);
+  m->tc_status.alloc(1);
+  OS_CUDA(cudaMemset(m->tc_status.get(), 0, sizeof(int)));
+  OS_CUDA(cudaFuncSetAttribute(gemm_ch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM));
   m->cap = np;
 }
 
-// out (np x 64, FP32) = A (np x np, BF16) B (np x 64, BF16) on the tensor
-// cores, K split over S CTAs per row block (np / 64 x S CTAs) and the S
+// out (np x 64, FP32) = A (np x np, BF16) B (np x 64, BF16, given transposed
+// as BT) on the tensor cores, K split over S CTAs per 128-row block and the S
 // partial products summed in order.
-void gemm_ch(os_mpnn *m, const __nv_bfloat16 *A, int np, const __nv_bfloat16 *B, float *out, cudaStream_t s) {
-  const int S = np % 128 == 0 ? 4 : 2;  // np is a multiple of 64: np / S is a multiple of 32
-  gemm_ch_kernel<<<dim3((unsigned)(np / GM), (unsigned)S), 128, 0, s>>>(A, np, np / S, B, m->gpart.get());
+void gemm_ch(os_mpnn *m, const __nv_bfloat16 *A, int np, const __nv_bfloat16 *BT, float *out, cudaStream_t s) {
+  const int chunks = np / TK;  // np is a multiple of 64
+  const int S = chunks % 4 == 0 ? 4 : chunks % 2 == 0 ? 2 : 1;
+  gemm_ch_kernel<<<dim3((unsigned)((np + TM - 1) / TM), (unsigned)S), 128, TC_SMEM, s>>>(
+      A, np, np / S, BT, m->gpart.get(), m->tc_status.get());
   OS_CUDA(cudaGetLastError());
   const size_t count = (size_t)np * GN;
   sum_parts_kernel<<<(unsigned)ceil_div_u64(count, 256), 256, 0, s>>>(m->gpart.get(), S, count, out);
   OS_CUDA(cudaGetLastError());
+}
+
+// OS_TIMEOUT if a tensor-core kernel's bounded wait ran out (after a
+// synchronisation of the context's stream); the flag is cleared.
+void check_tc_status(os_mpnn *m) {
+  int st = 0;
+  OS_CUDA(cudaMemcpy(&st, m->tc_status.get(), sizeof st, cudaMemcpyDeviceToHost));
+  if (st) {
+    OS_CUDA(cudaMemset(m->tc_status.get(), 0, sizeof(int)));
+    throw_error(OS_TIMEOUT, "a tensor-core message product's bounded wait ran out");
+  }
 }
 
 // Forward pass of instance `in` (activations kept for the backward pass).
@@ -389,7 +444,7 @@ void forward(os_mpnn *m, MpnnInstance &in, cudaStream_t s) {
   for (int l = 0; l < m->L; ++l) {
     const float *Hprev = m->Hs.get() + (size_t)l * nh;
     float *Ml = m->M.get() + (size_t)l * nh;
-    to_bf16_kernel<<<(unsigned)ceil_div_u64(nh, 256), 256, 0, s>>>(Hprev, m->Hb.get(), nh);
+    to_bf16_t_kernel<<<(unsigned)ceil_div_u64(nh, 256), 256, 0, s>>>(Hprev, m->Hb.get(), np, np);
     gemm_ch(m, in.c.get(), np, m->Hb.get(), Ml, s);
     const float *Wl = P + m->off_layer(l);
     linear_kernel<<<n, H, 0, s>>>(Hprev, Wl, Ml, Wl + (size_t)H * H, Wl + 2 * (size_t)H * H, n, H, H, 1,
@@ -425,7 +480,7 @@ void backward(os_mpnn *m, MpnnInstance &in, cudaStream_t s) {
     linear_back_kernel<<<n, H, 0, s>>>(m->dZ.get(), Wl + (size_t)H * H, n, H, H, 0, m->dM.get());
     linear_back_kernel<<<n, H, 0, s>>>(m->dZ.get(), Wl, n, H, H, 0, m->dH.get());
     OS_CUDA(cudaMemsetAsync(m->Hb.get(), 0, sizeof(__nv_bfloat16) * nh, s));
-    to_bf16_kernel<<<eb, 256, 0, s>>>(m->dM.get(), m->Hb.get(), rh);
+    to_bf16_t_kernel<<<eb, 256, 0, s>>>(m->dM.get(), m->Hb.get(), n, np);
     gemm_ch(m, in.c.get(), np, m->Hb.get(), m->dZ.get(), s);
     add_kernel<<<eb, 256, 0, s>>>(m->dH.get(), m->dZ.get(), rh);
   }
@@ -716,6 +771,7 @@ os_status os_mpnn_loss_grad(os_mpnn *m, int32_t index, float *loss, float *grads
       OS_CUDA(cudaMemcpyAsync(grads, m->grad.get(), sizeof(float) * m->nparam, cudaMemcpyDeviceToHost, s));
     }
     OS_CUDA(cudaStreamSynchronize(s));
+    check_tc_status(m);
   });
 }
 
@@ -762,8 +818,60 @@ os_status os_mpnn_train(os_mpnn *m, int32_t epochs, float lr, uint64_t shuffle_s
       }
     }
     OS_CUDA(cudaStreamSynchronize(s));
+    if (m->tc_status.count) check_tc_status(m);
   });
 }
+
+}  // extern "C"
+
+namespace {
+
+// Persistent prediction buffers and one captured graph per size: the
+// staging (from m->ptmp.f), its 112 power-iteration launches and the forward
+// pass replay as one launch, which leaves P(x_i = 1) in m->prob.
+void predict_prepare(os_mpnn *m, int n, cudaStream_t s) {
+  if (!m->pin || m->pin->n != n) {
+    m->pin = std::make_unique<MpnnInstance>();
+    stage_alloc(*m->pin, m->ptmp, n);
+  }
+  MpnnInstance &in = *m->pin;
+  ensure_work(m, in.np);
+  if (m->pgraph && (m->pgraph_n != n || m->pgraph_cap != m->cap)) {
+    cudaGraphExecDestroy(m->pgraph);
+    m->pgraph = nullptr;
+  }
+  if (!m->pgraph) {
+    cudaGraph_t g = nullptr;
+    OS_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    try {
+      stage_enqueue(in, m->ptmp, s);
+      forward(m, in, s);
+      const float *HL = m->Hs.get() + (size_t)m->L * in.np * m->H;
+      float *P = m->param.get();
+      head_kernel<<<(n + 255) / 256, 256, 0, s>>>(HL, P + m->off_wout(), P + m->off_bout(), nullptr, n, m->H,
+                                                  m->prob.get(), nullptr, nullptr);
+    } catch (...) {
+      // leave the stream out of capture mode before reporting
+      cudaStreamEndCapture(s, &g);
+      if (g) cudaGraphDestroy(g);
+      (void)cudaGetLastError();
+      throw;
+    }
+    const cudaError_t le = cudaGetLastError();
+    const cudaError_t ce = cudaStreamEndCapture(s, &g);
+    OS_CUDA(le);
+    OS_CUDA(ce);
+    const cudaError_t ie = cudaGraphInstantiate(&m->pgraph, g, 0);
+    cudaGraphDestroy(g);
+    OS_CUDA(ie);
+    m->pgraph_n = n;
+    m->pgraph_cap = m->cap;
+  }
+}
+
+}  // namespace
+
+extern "C" {
 
 os_status os_mpnn_predict(os_mpnn *m, const os_qubo_dense *q, float *prob) {
   return guard([&] {
@@ -772,52 +880,36 @@ os_status os_mpnn_predict(os_mpnn *m, const os_qubo_dense *q, float *prob) {
     cudaStream_t s = m->ctx->stream;
     const int n = q->n;
     OS_REQUIRE(n >= 2 && n <= 8192, "the network takes 2..8192 spins (got %d)", n);
-    // Persistent buffers and one captured graph per size: the staging, its
-    // 112 power-iteration launches and the forward pass replay as one launch.
-    if (!m->pin || m->pin->n != n) {
-      m->pin = std::make_unique<MpnnInstance>();
-      stage_alloc(*m->pin, m->ptmp, n);
-    }
-    MpnnInstance &in = *m->pin;
-    ensure_work(m, in.np);
-    if (m->pgraph && (m->pgraph_n != n || m->pgraph_cap != m->cap)) {
-      cudaGraphExecDestroy(m->pgraph);
-      m->pgraph = nullptr;
-    }
+    predict_prepare(m, n, s);
     OS_CUDA(cudaMemcpyAsync(m->ptmp.f.get(), q->f, sizeof(double) * (size_t)n * n, cudaMemcpyHostToDevice, s));
-    if (!m->pgraph) {
-      cudaGraph_t g = nullptr;
-      OS_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-      try {
-        stage_enqueue(in, m->ptmp, s);
-        forward(m, in, s);
-        const float *HL = m->Hs.get() + (size_t)m->L * in.np * m->H;
-        float *P = m->param.get();
-        head_kernel<<<(n + 255) / 256, 256, 0, s>>>(HL, P + m->off_wout(), P + m->off_bout(), nullptr, n, m->H,
-                                                    m->prob.get(), nullptr, nullptr);
-      } catch (...) {
-        // leave the stream out of capture mode before reporting
-        cudaStreamEndCapture(s, &g);
-        if (g) cudaGraphDestroy(g);
-        (void)cudaGetLastError();
-        throw;
-      }
-      const cudaError_t le = cudaGetLastError();
-      const cudaError_t ce = cudaStreamEndCapture(s, &g);
-      OS_CUDA(le);
-      OS_CUDA(ce);
-      const cudaError_t ie = cudaGraphInstantiate(&m->pgraph, g, 0);
-      cudaGraphDestroy(g);
-      OS_CUDA(ie);
-      m->pgraph_n = n;
-      m->pgraph_cap = m->cap;
-    }
     OS_CUDA(cudaGraphLaunch(m->pgraph, s));
     OS_CUDA(cudaMemcpyAsync(prob, m->prob.get(), sizeof(float) * n, cudaMemcpyDeviceToHost, s));
     double bad = 0.0;
     OS_CUDA(cudaMemcpyAsync(&bad, m->ptmp.stats.get() + 1, sizeof(double), cudaMemcpyDeviceToHost, s));
     OS_CUDA(cudaStreamSynchronize(s));
+    check_tc_status(m);
     OS_REQUIRE(bad == 0.0, "the QUBO has non-finite coefficients");
+  });
+}
+
+os_status os_sa_plan_warm_start(os_sa_plan *p, os_mpnn *m) {
+  return guard([&] {
+    OS_REQUIRE(p && m, "null argument");
+    OS_REQUIRE(p->kind == 0, "the warm start takes a dense plan");
+    OS_REQUIRE(p->ctx == m->ctx, "the plan and the network must share a context");
+    activate(p->ctx);
+    cudaStream_t s = p->ctx->stream;
+    const int n = p->n;
+    OS_REQUIRE(n >= 2 && n <= 8192, "the network takes 2..8192 spins (got %d)", n);
+    predict_prepare(m, n, s);
+    // The plan's matrix as given is already on the device (and was checked
+    // finite when the plan was created): a device copy into the staging
+    // buffer, the graph, and the probabilities straight into the plan.
+    OS_CUDA(cudaMemcpyAsync(m->ptmp.f.get(), p->f.get(), sizeof(double) * (size_t)n * n, cudaMemcpyDeviceToDevice,
+                            s));
+    OS_CUDA(cudaGraphLaunch(m->pgraph, s));
+    if (p->init_prob.count != (size_t)n) p->init_prob.alloc(n);
+    OS_CUDA(cudaMemcpyAsync(p->init_prob.get(), m->prob.get(), sizeof(float) * n, cudaMemcpyDeviceToDevice, s));
   });
 }
 

@@ -31,7 +31,7 @@ from typing import Optional, Sequence
 
 import numpy as np
 
-from . import (ACCEPT_PHYSICAL, BatchedAnnealPlan, Context, WarmStartNet, anneal, default_context,
+from . import (ACCEPT_PHYSICAL, AnnealPlan, BatchedAnnealPlan, Context, WarmStartNet, anneal, default_context,
                geometric_schedule)
 
 
@@ -141,19 +141,30 @@ class TTT:
     energies: dict = field(default_factory=dict)
 
 
-def time_to_target(f: np.ndarray, target: float, *, rel_gap: float = 0.005, init_prob=None,
+def time_to_target(f: np.ndarray, target: float, *, rel_gap: float = 0.005, init_prob=None, net=None,
                    budgets: Sequence[int] = (25, 35, 50, 70, 100, 140, 200, 280, 400, 800, 1600),
                    num_tries: int = 512,
                    beta_min: float = 0.1, beta_max: float = 5.0, seed: int = 21,
                    ctx: Optional[Context] = None) -> TTT:
-    """Smallest sweep budget whose best energy is within rel_gap of target."""
+    """Smallest sweep budget whose best energy is within rel_gap of target.
+    Each try is one whole anneal through the C ABI (upload, kernels, answer);
+    with `net`, the try also predicts the warm start on the device from the
+    plan's own matrix (AnnealPlan.warm_start), inside the timed region."""
     thr = target + rel_gap * abs(target)
     res = TTT(None, None)
     for s in budgets:
         beta = geometric_schedule(beta_min, beta_max, s)
         t0 = time.perf_counter()
-        r = anneal(f, beta, num_tries=num_tries, site_order=1, acceptance=ACCEPT_PHYSICAL, init_prob=init_prob,
-                   resync_every=-1, seed=seed, ctx=ctx)  # no drift check: every arm only wants its best energy
+        if net is not None:
+            plan = AnnealPlan(f, beta, num_tries=num_tries, site_order=1, acceptance=ACCEPT_PHYSICAL,
+                              resync_every=-1, seed=seed, ctx=ctx)
+            plan.warm_start(net)
+            plan.execute()
+            r = plan.result()
+            plan.close()
+        else:
+            r = anneal(f, beta, num_tries=num_tries, site_order=1, acceptance=ACCEPT_PHYSICAL, init_prob=init_prob,
+                       resync_every=-1, seed=seed, ctx=ctx)  # no drift check: every arm only wants its best energy
         dt = time.perf_counter() - t0
         res.energies[s] = r.energy
         if r.energy <= thr:

@@ -103,6 +103,33 @@ def test_shipped_network_beats_fair_coins_on_sk(native, ctx):
 
 
 @pytest.mark.gpu
+def test_plan_warm_start_equals_host_prediction(native, ctx):
+    """os_sa_plan_warm_start (the network on the plan's device-resident
+    matrix, probabilities straight into the plan) starts the same trajectories
+    as passing the host-path prediction as init_prob."""
+    from onesolver_gb300 import warmstart as ws
+    sh = ws.load_shipped(ctx)
+    f = ws.sk_qubo(1024, int(sh.eval_seeds[0]))
+    beta = native.geometric_schedule(2.0, 5.0, 30)
+    prob = sh.net.predict(f)
+    a = native.AnnealPlan(f, beta, num_tries=256, acceptance=1, init_prob=prob, seed=4, ctx=ctx)
+    b = native.AnnealPlan(f, beta, num_tries=256, acceptance=1, seed=4, ctx=ctx)
+    b.warm_start(sh.net)
+    for p in (a, b):
+        p.execute()
+    ra, rb = a.result(traj_states=True), b.result(traj_states=True)
+    assert np.array_equal(ra.traj_energies, rb.traj_energies)
+    assert np.array_equal(ra.traj_states, rb.traj_states)
+    a.close(), b.close()
+    g = random_normal_qubo(64, 1)
+    sp = native.AnnealPlan(native.Csr.from_dense(g), beta, num_tries=8, ctx=ctx)
+    with pytest.raises(native.OneSolverError):
+        sp.warm_start(sh.net)   # dense plans only
+    sp.close()
+    sh.net.close()
+
+
+@pytest.mark.gpu
 def test_training_learns_and_warm_start_gains(native, orc, ctx):
     net = native.WarmStartNet(ctx=ctx, seed=7, orient=False)
     for s in range(24):
