@@ -296,9 +296,9 @@ def bench_exhaustive(args, ctx, pg, rank, world):
     d2h = 56 + 8 * min(r.count, 1 << 16)
 
     k_ms = statistics.mean(kern_ms)
-    # Matched ceiling: the issue rate of the instructions this plan's variant
-    # spends per state (packed variant: two states per add), measured in this
-    # run; MEASURED_PEAKS.json has no integer figure.
+    # Matched ceiling: this plan's variant's own inner block walk (the
+    # kernel's instruction sequence without per-item bookkeeping), measured in
+    # this run; MEASURED_PEAKS.json has no integer figure.
     variant = plan.variant
     peak = osg.probe_exhaustive_pair(variant, ctx)
     achieved = states / (k_ms * 1e-3)
@@ -316,8 +316,9 @@ def bench_exhaustive(args, ctx, pg, rank, world):
                      "frac": achieved / peak, "traffic": TRAFFIC.get("exhaustive36"),
                      "variant": variant, "ops_per_unit": 2, "kernel_ms": k_ms,
                      "states_per_sm_clock": achieved / (sms * load_peaks().get("sm_max_mhz", 2070.0) * 1e6),
-                     "peak_source": ("os_probe_exhaustive_pair(%d): the issue rate of this variant's per-state "
-                                     "instructions, measured in this run (MEASURED_PEAKS.json has no integer "
+                     "peak_source": ("os_probe_exhaustive_pair(%d): this variant's own inner block walk (the "
+                                     "kernel's instruction sequence, couplings changing per block, no per-item "
+                                     "bookkeeping), measured in this run (MEASURED_PEAKS.json has no integer "
                                      "figure)" % variant)},
         "e2e": {"value": world * states / e2e_step, "unit": "states/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "ms_per_step": e2e_step * 1e3},
@@ -655,7 +656,7 @@ def bench_learned(args, ctx, pg, rank, world):
                                f"beta 0.1->5.0 from fair coins; the warm start and its control (fair coins) both run "
                                f"beta {WARM_BETA_MIN}->5.0; the probe gate compares those two",
                    "network": "3 message-passing layers, hidden 64, BF16 tensor-core messages + FP32; node "
-                              "features: diagonal, row sum, anchor spin, FP64 power-iteration low-spectrum vector"},
+                              "features: diagonal, row sum, anchor spin, power-iteration low-spectrum vector (FP32 products, FP64 norms)"},
         "result": {"instances": len(rows), "solved_by_all_arms": len(both),
                    "plain_median_s": med("plain_s", both), "cold_schedule_random_median_s": med("cold_s", both),
                    "warm_median_s": med("warm_s", both), "predict_median_s": med("predict_s"),

@@ -606,12 +606,13 @@ os_status os_sa_plan_warm_start(os_sa_plan *plan, os_mpnn *model);
  * and the shared-memory read rate of the annealing field update (128-bit
  * shared loads feeding paired FP32 FMAs), in GB/s. No reference counterpart. */
 os_status os_probe_int32_peak(os_ctx *ctx, double *gops);
-/* States per second at the issue rate of exhaustive variant `variant`'s
- * per-state instructions (1: three-input add + min; 2: multiply-add + fused
- * add-min; 3: packed 16-bit halves, a three-input add per two states and a
- * three-input per-half minimum per four), four independent chains per thread
- * at full occupancy: the ceiling of the enumeration's inner loop without its
- * bookkeeping. */
+/* States per second of exhaustive variant `variant`'s own inner block walk
+ * (1: three-input add + min; 2: multiply-add + fused add-min; 3: packed
+ * 16-bit halves, a three-input add per two states and a three-input per-half
+ * minimum per four), the enumeration kernel's instruction sequence run block
+ * after block at full occupancy, with couplings that change between blocks as
+ * they do in the enumeration: the ceiling of the enumeration's inner loop
+ * without its per-item bookkeeping. */
 os_status os_probe_exhaustive_pair(os_ctx *ctx, int32_t variant, double *states_per_s);
 os_status os_probe_fp32_fma_peak(os_ctx *ctx, double *gflops);
 os_status os_probe_smem_row_peak(os_ctx *ctx, double *gbs);

@@ -1100,8 +1100,9 @@ def probe_int32_peak(ctx: Optional[Context] = None) -> float:
 
 
 def probe_exhaustive_pair(variant: int, ctx: Optional[Context] = None) -> float:
-    """States/s at the issue rate of exhaustive variant `variant`'s per-state
-    instructions (1, 2 or 3; 3 = packed, two states per add)."""
+    """States/s of exhaustive variant `variant`'s own inner block walk (1, 2
+    or 3; 3 = packed, two states per add): the enumeration's instruction
+    sequence without its per-item bookkeeping."""
     ctx = ctx or default_context()
     v = C.c_double()
     _check(lib().os_probe_exhaustive_pair(ctx.handle, variant, C.byref(v)))

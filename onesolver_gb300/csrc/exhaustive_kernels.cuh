@@ -31,7 +31,7 @@ constexpr int INNER_MAX = 1 << G_MAX;
 constexpr int LCAP = 4;              // states kept per thread
 constexpr int THREADS = 256;         // threads per CTA
 constexpr int CTA_CAP = 128;         // states kept per CTA
-constexpr int LOOP_BITS = 5;         // blocks per work item = 2^LOOP_BITS
+constexpr int LOOP_BITS = 6;         // blocks per work item = 2^LOOP_BITS
 constexpr int SMALL_FREE = 14;       // below: one thread per state
 constexpr int MAX_N = 50;
 constexpr uint64_t CAND_CAP = 1u << 20;  // fixed-point candidate buffer
@@ -413,7 +413,7 @@ __device__ __forceinline__ void process_item(unsigned long long item, const Gray
 // Its energy delta splits into bw[w] (its diagonal and its couplings to the
 // item's fixed set bits, summed once per item in the pass that builds the
 // coupling vector) plus its couplings to the other walked bits that are set
-// (at most three loads), instead of a row sum over every set bit per flip.
+// (at most W - 1 loads), instead of a row sum over every set bit per flip.
 template <int G>
 __device__ __forceinline__ void process_item_packed(unsigned long long item, const GrayParams<int> &P,
                                                     ThreadBest<int> &tb, CollectState &cs) {
@@ -423,7 +423,7 @@ __device__ __forceinline__ void process_item_packed(unsigned long long item, con
   const int *__restrict__ rowt = q + (size_t)top * n;
   unsigned long long xa = P.prefix_state | (item << (G + P.loop_bits));
   const int Ea = energy_from_scratch(q, n, xa);
-  const int W = P.loop_bits - 1;  // walked bits G .. G + W - 1 (W <= LOOP_BITS - 1 = 4)
+  const int W = P.loop_bits - 1;  // walked bits G .. G + W - 1 (W <= LOOP_BITS - 1)
   int ca[G];
 #pragma unroll
   for (int i = 0; i < G; ++i) ca[i] = 0;

@@ -12,7 +12,8 @@
 //   X       = [1, d_i / s, r_i / s, [i == 0], u_i] node features: diagonal
 //             d_i, row sum r_i of C, scale s = rms(C) sqrt(n); spin 0 is the
 //             anchor; u = sqrt(n) v sign(v_0), v the unit vector that power
-//             iteration on (sigma I - C / s) reaches in FP64 (spectral_feature):
+//             iteration on (sigma I - C / s) reaches (FP32 products, FP64
+//             norms; spec_step_kernel):
 //             the low end of the coupling spectrum, which the ground states of
 //             field-free couplings follow (min over s of s^T C s)
 //   H0      = relu(X W_in + b_in)
@@ -304,42 +305,116 @@ __global__ void adam_kernel(float *__restrict__ p, const float *__restrict__ g, 
 using namespace os;
 using namespace os::mpnn;
 
-// One stored instance: scaled couplings (BF16, padded to np x np), features,
-// optional labels.
-// One power-iteration step in FP64, a warp per row: out = C v^ (mode 0) or
-// sigma v^ - C v^ (mode 1, sigma read from the device), v^ = v / sqrt(*norm_in);
-// the squared norm of out accumulates into *norm_out.
-__global__ void __launch_bounds__(256) spec_step_kernel(const double *__restrict__ c, int n,
-                                                        const double *__restrict__ v,
-                                                        const double *__restrict__ norm_in,
-                                                        const double *__restrict__ sigma_p, int mode,
-                                                        double *__restrict__ out, double *__restrict__ norm_out) {
-  const int row = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  const int lane = threadIdx.x & 31;
-  if (row >= n) return;
-  const double inv = *norm_in > 0.0 ? 1.0 / sqrt(*norm_in) : 0.0;
-  const double *cr = c + (size_t)row * n;
-  double acc = 0.0;
-  for (int j = lane; j < n; j += 32) acc += cr[j] * v[j];
+// One step of the power-iteration chain, a warp per row, on the FP32 copy of
+// C^ (rows of `ld` floats, ld a multiple of 128, zero beyond n; v likewise
+// zero beyond n): out = C v^ (mode 0) or sigma v^ - C v^ (mode 1,
+// sigma = 1.05 sqrt(*rho2)), v^ = v / sqrt(*norm_in). Products accumulate in
+// FP32, the scaling and the squared norm of out in FP64; one atomic per CTA
+// adds the CTA's share of that norm into *norm_out. With `x` (the first
+// step) the step also stores the row sum of C^ as node feature 2. FP64
+// arithmetic is scarce on this part: the norm's reciprocal square root and
+// sigma are formed once per CTA, the FP64 products once per row.
+//
+// The steps are chained by programmatic dependent launch: a step may start
+// while its predecessor runs, loads its row of the matrix (which no step
+// writes) into registers, and only then waits for the predecessor's results
+// (griddepcontrol.wait); it releases its own successor after that wait, so a
+// step's early part never overlaps a step older than its predecessor. The
+// vector is read through L2 (ld.global.cg) into shared memory once per CTA.
+constexpr int SPEC_WARPS = 4;
+constexpr int SPEC_PRE = 8;  // float4 of the row per lane loaded before the wait (rows up to 1024)
+__global__ void __launch_bounds__(SPEC_WARPS * 32) spec_step_kernel(const float *__restrict__ c, int n, int ld,
+                                                                    const float *v, const double *norm_in,
+                                                                    const double *rho2, int mode, float *out,
+                                                                    double *norm_out, float *x) {
+  extern __shared__ float4 vs[];  // ld / 4
+  __shared__ double part[SPEC_WARPS], sc[2];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int row = blockIdx.x * SPEC_WARPS + warp;
+  const int q = ld >> 2;
+  const float4 *cr = reinterpret_cast<const float4 *>(c + (size_t)(row < n ? row : 0) * ld);
+  float4 pre[SPEC_PRE];
 #pragma unroll
-  for (int off = 16; off > 0; off >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
-  if (lane == 0) {
-    const double y = mode ? (*sigma_p * v[row] - acc) * inv : acc * inv;
-    out[row] = y;
-    atomicAdd(norm_out, y * y);
+  for (int t = 0; t < SPEC_PRE; ++t) {
+    const int j = lane + 32 * t;
+    pre[t] = row < n && j < q ? __ldg(cr + j) : make_float4(0.f, 0.f, 0.f, 0.f);
+  }
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+  if (threadIdx.x == 0) {
+    const double nin = __ldcg(norm_in);
+    sc[0] = nin > 0.0 ? 1.0 / sqrt(nin) : 0.0;
+    sc[1] = mode ? 1.05 * sqrt(__ldcg(rho2)) : 0.0;
+  }
+  const float4 *v4 = reinterpret_cast<const float4 *>(v);
+  for (int j = threadIdx.x; j < q; j += blockDim.x) vs[j] = __ldcg(v4 + j);
+  __syncthreads();
+  double y = 0.0;
+  if (row < n) {
+    float a0 = 0.f, a1 = 0.f, a2 = 0.f, a3 = 0.f;
+#pragma unroll
+    for (int t = 0; t < SPEC_PRE; ++t) {
+      const int j = lane + 32 * t;
+      if (j < q) {
+        const float4 vv = vs[j];
+        a0 = fmaf(pre[t].x, vv.x, a0);
+        a1 = fmaf(pre[t].y, vv.y, a1);
+        a2 = fmaf(pre[t].z, vv.z, a2);
+        a3 = fmaf(pre[t].w, vv.w, a3);
+      }
+    }
+#pragma unroll 4
+    for (int j = lane + 32 * SPEC_PRE; j < q; j += 32) {
+      const float4 cv = __ldg(cr + j), vv = vs[j];
+      a0 = fmaf(cv.x, vv.x, a0);
+      a1 = fmaf(cv.y, vv.y, a1);
+      a2 = fmaf(cv.z, vv.z, a2);
+      a3 = fmaf(cv.w, vv.w, a3);
+    }
+    float acc = (a0 + a1) + (a2 + a3);
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
+    if (x) {
+      float ls = 0.f;
+#pragma unroll
+      for (int t = 0; t < SPEC_PRE; ++t) ls += (pre[t].x + pre[t].y) + (pre[t].z + pre[t].w);
+      for (int j = lane + 32 * SPEC_PRE; j < q; j += 32) {
+        const float4 cv = __ldg(cr + j);
+        ls += (cv.x + cv.y) + (cv.z + cv.w);
+      }
+      double rsum = ls;
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) rsum += __shfl_xor_sync(0xffffffffu, rsum, off);
+      if (lane == 0) x[(size_t)row * FEAT + 2] = (float)rsum;
+    }
+    if (lane == 0) {
+      const double vr = reinterpret_cast<const float *>(vs)[row];
+      y = mode ? (sc[1] * vr - (double)acc) * sc[0] : (double)acc * sc[0];
+      out[row] = (float)y;
+    }
+  }
+  if (lane == 0) part[warp] = y * y;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+#pragma unroll
+    for (int w = 0; w < SPEC_WARPS; ++w) t += part[w];
+    atomicAdd(norm_out, t);
   }
 }
 
 // u_i = sqrt(n) v^_i sign(v^_0) into column `col` of the feature matrix.
-__global__ void spec_feature_kernel(const double *__restrict__ v, const double *__restrict__ norm, int n,
+__global__ void spec_feature_kernel(const float *__restrict__ v, const double *__restrict__ norm, int n,
                                     float *__restrict__ x, int col) {
+  __shared__ double fac;  // sqrt(n) sign(v_0) / |v|, formed once per CTA
+  if (threadIdx.x == 0) fac = (*norm > 0.0 ? sqrt((double)n / *norm) : 0.0) * (v[0] < 0.f ? -1.0 : 1.0);
+  __syncthreads();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const double inv = *norm > 0.0 ? 1.0 / sqrt(*norm) : 0.0;
-  const double sg = v[0] < 0.0 ? -1.0 : 1.0;
-  x[(size_t)i * FEAT + col] = (float)(sqrt((double)n) * v[i] * inv * sg);
+  if (i < n) x[(size_t)i * FEAT + col] = (float)(fac * (double)v[i]);
 }
 
+// One stored instance: scaled couplings (BF16, padded to np x np), features,
+// optional labels.
 struct MpnnInstance {
   int n = 0, np = 0;
   DevBuf<__nv_bfloat16> c;
@@ -347,10 +422,13 @@ struct MpnnInstance {
   DevBuf<uint8_t> y;   // n (oriented labels) or empty
 };
 
-// Temporaries of staging an instance: the matrix as given, FP64 scaled
-// couplings, power-iteration vectors and norms, coefficient statistics.
+// Temporaries of staging an instance: the matrix as given, FP32 scaled
+// couplings (rows padded to `ld`), power-iteration vectors, their FP64 norms,
+// coefficient statistics.
 struct StageTmp {
-  DevBuf<double> f, c64, v[3], norms, stats, sigma;
+  int ld = 0;
+  DevBuf<double> f, norms, stats, part;
+  DevBuf<float> c32, v[3];
 };
 
 struct os_mpnn {
@@ -492,84 +570,140 @@ void backward(os_mpnn *m, MpnnInstance &in, cudaStream_t s) {
 }
 
 // Start vector of the power iterations: positive, uneven, deterministic.
-// Start vector of the power iterations: positive, uneven, deterministic.
 __host__ __device__ inline double spec_start(int i) {
   return 1.0 + 0.25 * (double)(((uint32_t)i * 2654435761u) >> 24) / 255.0;
 }
 
-// stats[0] += squares of the off-diagonal upper-triangle coefficients,
-// stats[1] += count of non-finite coefficients on or above the diagonal.
-// A warp per row.
-__global__ void __launch_bounds__(256) stage_stats_kernel(const double *__restrict__ f, int n,
-                                                          double *__restrict__ stats) {
-  const int i = blockIdx.x * 8 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
-  if (i >= n) return;
+// Staging works on 32 x 32 tiles (I, J) of the upper triangle: a 2-D grid of
+// T x T CTAs (T = ceil(n / 32), blockIdx.y = I, blockIdx.x = J) in which the
+// CTAs below the diagonal return at once. Thread (ty, tx) = (warp, lane)
+// takes tile rows ty, ty + 8, ty + 16, ty + 24 at column tx.
+constexpr int STAGE_TILE = 32;
+
+// stats[0] = sum of squares of the off-diagonal upper-triangle coefficients,
+// stats[1] = count of non-finite coefficients on or above the diagonal. Each
+// tile's CTA writes its two partial sums to part[2 (I T + J)]; the last CTA
+// to finish (counted in *done, zero at launch) adds them in index order, so
+// the result does not depend on the order in which the CTAs ran.
+__global__ void __launch_bounds__(256) stage_stats_kernel(const double *__restrict__ f, int n, double *part,
+                                                          unsigned *done, double *__restrict__ stats) {
+  const int T = gridDim.x, I = blockIdx.y, J = blockIdx.x;
+  if (I > J) return;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  __shared__ double rs[8], rb[8];
+  __shared__ bool last;
   double ss = 0.0, bad = 0.0;
-  for (int j = i + lane; j < n; j += 32) {
-    const double v = f[(size_t)i * n + j];
-    if (!isfinite(v)) bad += 1.0;
-    else if (j > i) ss += v * v;
+  const int gj = J * STAGE_TILE + tx;
+#pragma unroll
+  for (int r = ty; r < STAGE_TILE; r += 8) {
+    const int gi = I * STAGE_TILE + r;
+    if (gi < n && gj < n && gj >= gi) {
+      const double v = f[(size_t)gi * n + gj];
+      if (!isfinite(v)) bad += 1.0;
+      else if (gj > gi) ss += v * v;
+    }
   }
 #pragma unroll
   for (int off = 16; off > 0; off >>= 1) {
     ss += __shfl_xor_sync(0xffffffffu, ss, off);
     bad += __shfl_xor_sync(0xffffffffu, bad, off);
   }
-  if (lane == 0) {
-    atomicAdd(&stats[0], ss);
-    if (bad > 0.0) atomicAdd(&stats[1], bad);
+  if (tx == 0) rs[ty] = ss, rb[ty] = bad;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double a = 0.0, b = 0.0;
+    for (int w = 0; w < 8; ++w) a += rs[w], b += rb[w];
+    part[2 * ((size_t)I * T + J)] = a;
+    part[2 * ((size_t)I * T + J) + 1] = b;
+    __threadfence();
+    last = atomicAdd(done, 1u) == (unsigned)(T * (T + 1) / 2 - 1);
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  double a = 0.0, b = 0.0;
+  for (int k = threadIdx.x; k < T * T; k += blockDim.x)
+    if (k / T <= k % T) a += __ldcg(part + 2 * (size_t)k), b += __ldcg(part + 2 * (size_t)k + 1);
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    a += __shfl_xor_sync(0xffffffffu, a, off);
+    b += __shfl_xor_sync(0xffffffffu, b, off);
+  }
+  if (tx == 0) rs[ty] = a, rb[ty] = b;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double ta = 0.0, tb = 0.0;
+    for (int w = 0; w < 8; ++w) ta += rs[w], tb += rb[w];
+    stats[0] = ta;
+    stats[1] = tb;
   }
 }
 
-// Scaled symmetric couplings C^ = C / s (BF16, np-padded, and FP64) and the
-// node features of row i (a warp per row); s = rms * sqrt(n) from stats[0]
-// over `pairs` coefficients (1 when they are all zero). The start vector of
-// the power iterations goes to v0, its squared norm to *norm0.
-__global__ void __launch_bounds__(256) stage_build_kernel(const double *__restrict__ f, int n, int np, double pairs,
-                                                          const double *__restrict__ stats,
-                                                          __nv_bfloat16 *__restrict__ cb, double *__restrict__ c64,
-                                                          float *__restrict__ x, double *__restrict__ v0,
-                                                          double *__restrict__ norm0) {
-  const int i = blockIdx.x * 8 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
-  if (i >= n) return;
-  const double rms = pairs > 0 ? sqrt(stats[0] / pairs) : 0.0;
-  const double scale = rms > 0 ? rms * sqrt((double)n) : 1.0;
-  double rowsum = 0.0;
-  for (int j = lane; j < n; j += 32) {
-    double v = 0.0;
-    if (j != i) v = i < j ? f[(size_t)i * n + j] : f[(size_t)j * n + i];
-    rowsum += v;
-    cb[(size_t)i * np + j] = __float2bfloat16((float)(v / scale));
-    c64[(size_t)i * n + j] = v / scale;
+// Scaled symmetric couplings C^ = C / s, s = rms * sqrt(n) from stats[0]
+// over `pairs` coefficients (1 when they are all zero), from the upper
+// triangle of f: BF16 with rows of np and FP32 with rows of ld (both
+// zero-filled beforehand; only entries below n are written). Tile (I, J)
+// writes block (I, J) and, through a shared-memory transpose, block (J, I).
+// The diagonal tiles write the node features that need no row sum (the row
+// sums are added by the first power-iteration step) and the start vector of
+// the power iterations; CTA (0, 0) stores its squared norm, `start_norm`.
+__global__ void __launch_bounds__(256) stage_build_kernel(const double *__restrict__ f, int n, int np, int ld,
+                                                          double pairs, const double *__restrict__ stats,
+                                                          __nv_bfloat16 *__restrict__ cb, float *__restrict__ c32,
+                                                          float *__restrict__ x, float *__restrict__ v0,
+                                                          double start_norm, double *__restrict__ norm0) {
+  const int I = blockIdx.y, J = blockIdx.x;
+  if (I > J) return;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  __shared__ double tile[STAGE_TILE][STAGE_TILE + 1];
+  __shared__ double scale_s[2];  // s and 1 / s, formed once per CTA (FP64 is scarce)
+  if (threadIdx.x == 0) {
+    const double rms = pairs > 0 ? sqrt(stats[0] / pairs) : 0.0;
+    scale_s[0] = rms > 0 ? rms * sqrt((double)n) : 1.0;
+    scale_s[1] = 1.0 / scale_s[0];
   }
 #pragma unroll
-  for (int off = 16; off > 0; off >>= 1) rowsum += __shfl_xor_sync(0xffffffffu, rowsum, off);
-  if (lane == 0) {
-    float *xi = x + (size_t)i * FEAT;
-    xi[0] = 1.f;
-    xi[1] = (float)(f[(size_t)i * n + i] / scale);
-    xi[2] = (float)(rowsum / scale);
-    xi[3] = i == 0 ? 1.f : 0.f;
-    xi[4] = 0.f;
-    const double s0 = spec_start(i);
-    v0[i] = s0;
-    atomicAdd(norm0, s0 * s0);
+  for (int r = ty; r < STAGE_TILE; r += 8) {
+    const int gi = I * STAGE_TILE + r, gj = J * STAGE_TILE + tx;
+    tile[r][tx] = gi < n && gj < n && gi < gj ? f[(size_t)gi * n + gj] : 0.0;
+  }
+  __syncthreads();
+  const double inv_scale = scale_s[1];
+#pragma unroll
+  for (int r = ty; r < STAGE_TILE; r += 8) {
+    int gi = I * STAGE_TILE + r, gj = J * STAGE_TILE + tx;
+    if (gi < n && gj < n) {
+      const double v = (I == J && r > tx ? tile[tx][r] : tile[r][tx]) * inv_scale;
+      c32[(size_t)gi * ld + gj] = (float)v;
+      cb[(size_t)gi * np + gj] = __float2bfloat16((float)v);
+    }
+    gi = J * STAGE_TILE + r, gj = I * STAGE_TILE + tx;
+    if (I < J && gi < n && gj < n) {
+      const double v = tile[tx][r] * inv_scale;
+      c32[(size_t)gi * ld + gj] = (float)v;
+      cb[(size_t)gi * np + gj] = __float2bfloat16((float)v);
+    }
+  }
+  if (I == J && ty == 0) {
+    const int i = I * STAGE_TILE + tx;
+    if (i < n) {
+      float *xi = x + (size_t)i * FEAT;
+      xi[0] = 1.f;
+      xi[1] = (float)(f[(size_t)i * n + i] / scale_s[0]);
+      xi[3] = i == 0 ? 1.f : 0.f;
+      xi[4] = 0.f;
+      v0[i] = (float)spec_start(i);
+    }
+    if (I == 0 && tx == 0) *norm0 = start_norm;
   }
 }
 
-// sigma = 1.05 * rho, rho = sqrt(*rho2) (the norm of C^ v^ after the
-// spectral-radius iterations).
-__global__ void spec_sigma_kernel(const double *__restrict__ rho2, double *__restrict__ sigma) {
-  *sigma = 1.05 * sqrt(*rho2);
-}
-
-
-// Stage an instance on `s`: the QUBO goes up once; scale, BF16 and FP64
+// Stage an instance on `s`: the QUBO goes up once; scale, BF16 and FP32
 // scaled couplings, node features and the spectral feature are computed on
 // the device. The spectral feature (column 4): SPEC_RHO_ITERS power
 // iterations on C^ estimate its spectral radius rho, then SPEC_ITERS
-// iterations on (1.05 rho I - C^) from the same start vector, FP64
-// throughout, no host round trip. With a label the stream is synchronised,
+// iterations on (1.05 rho I - C^) from the same start vector (FP32 products
+// from the L2-resident FP32 matrix, FP64 norms), no host round trip. With a label the stream is synchronised,
 // the coefficients checked and the label oriented; without one the caller
 // checks `tmp.stats[1]` (non-finite count) after its own synchronisation.
 // Device buffers of an instance of n spins and of its staging.
@@ -577,14 +711,16 @@ void stage_alloc(MpnnInstance &in, StageTmp &tmp, int n) {
   in.n = n;
   in.np = (n + 63) / 64 * 64;
   const size_t nn = (size_t)n * n;
+  tmp.ld = (n + 127) / 128 * 128;
   tmp.f.alloc(nn);
-  tmp.stats.alloc(2);
+  tmp.stats.alloc(3);
+  const size_t T = (n + STAGE_TILE - 1) / STAGE_TILE;
+  tmp.part.alloc(2 * T * T);
   tmp.norms.alloc(SPEC_RHO_ITERS + SPEC_ITERS + 2);
-  tmp.sigma.alloc(1);
   in.c.alloc((size_t)in.np * in.np);
-  tmp.c64.alloc(nn);
+  tmp.c32.alloc((size_t)n * tmp.ld);
   in.x.alloc((size_t)n * FEAT);
-  for (auto &b : tmp.v) b.alloc(n);
+  for (auto &b : tmp.v) b.alloc(tmp.ld);
 }
 
 // Staging kernels on `s` (tmp.f already holds the matrix): no allocation and
@@ -592,35 +728,59 @@ void stage_alloc(MpnnInstance &in, StageTmp &tmp, int n) {
 void stage_enqueue(MpnnInstance &in, StageTmp &tmp, cudaStream_t s) {
   const int n = in.n;
   const int total = SPEC_RHO_ITERS + SPEC_ITERS + 2;
-  OS_CUDA(cudaMemsetAsync(tmp.stats.get(), 0, sizeof(double) * 2, s));
+  OS_CUDA(cudaMemsetAsync(tmp.stats.get(), 0, sizeof(double) * 3, s));  // sums, non-finite count, CTA counter
   OS_CUDA(cudaMemsetAsync(tmp.norms.get(), 0, sizeof(double) * total, s));
   OS_CUDA(cudaMemsetAsync(in.c.get(), 0, sizeof(__nv_bfloat16) * in.c.count, s));
-  const int rows = (n + 7) / 8;
-  stage_stats_kernel<<<rows, 256, 0, s>>>(tmp.f.get(), n, tmp.stats.get());
+  for (auto &b : tmp.v) OS_CUDA(cudaMemsetAsync(b.get(), 0, sizeof(float) * b.count, s));
+  OS_CUDA(cudaMemsetAsync(tmp.c32.get(), 0, sizeof(float) * tmp.c32.count, s));
+  const int T = (n + STAGE_TILE - 1) / STAGE_TILE;
+  const dim3 tiles(T, T);
+  stage_stats_kernel<<<tiles, 256, 0, s>>>(tmp.f.get(), n, tmp.part.get(),
+                                           reinterpret_cast<unsigned *>(tmp.stats.get() + 2), tmp.stats.get());
   OS_CUDA(cudaGetLastError());
-  stage_build_kernel<<<rows, 256, 0, s>>>(tmp.f.get(), n, in.np, (double)n * (n - 1) / 2, tmp.stats.get(),
-                                          in.c.get(), tmp.c64.get(), in.x.get(), tmp.v[2].get(), tmp.norms.get());
+  double start_norm = 0.0;  // of the start vector as stored (FP32), in index order
+  for (int i = 0; i < n; ++i) {
+    const double v = (double)(float)spec_start(i);
+    start_norm += v * v;
+  }
+  stage_build_kernel<<<tiles, 256, 0, s>>>(tmp.f.get(), n, in.np, tmp.ld, (double)n * (n - 1) / 2,
+                                           tmp.stats.get(), in.c.get(), tmp.c32.get(), in.x.get(), tmp.v[2].get(),
+                                           start_norm, tmp.norms.get());
   OS_CUDA(cudaGetLastError());
-  // Power iterations: step k reads v[k & 1] (v[2] = the start vector for
-  // k = 0) with its squared norm in norms[slot0 + k] and writes the next.
-  auto run = [&](int iters, int mode, int slot0) {
+  // Power iterations, one chain of SPEC_RHO_ITERS + SPEC_ITERS steps. Step k
+  // of a phase reads v[k & 1] (v[2], the start vector, for k = 0) and writes
+  // v[(k + 1) & 1]. Squared norms: norms[0] is the start vector's; the C^
+  // phase writes norms[1 .. R] (R = SPEC_RHO_ITERS, rho^2 = norms[R]); the
+  // (sigma I - C^) phase writes norms[R + 1 .. R + SPEC_ITERS], its first
+  // step reading norms[0] again.
+  const int R = SPEC_RHO_ITERS;
+  cudaLaunchAttribute chain;
+  chain.id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  chain.val.programmaticStreamSerializationAllowed = 1;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((n + SPEC_WARPS - 1) / SPEC_WARPS);
+  cfg.blockDim = dim3(SPEC_WARPS * 32);
+  cfg.dynamicSmemBytes = sizeof(float) * tmp.ld;
+  cfg.stream = s;
+  cfg.attrs = &chain;
+  double *norms = tmp.norms.get();
+  int last = 0;
+  for (int mode = 0; mode < 2; ++mode) {
+    const int iters = mode ? SPEC_ITERS : R, slot0 = mode ? R : 0;
     for (int k = 0; k < iters; ++k) {
-      const double *vin = k == 0 ? tmp.v[2].get() : tmp.v[k & 1].get();
-      spec_step_kernel<<<rows, 256, 0, s>>>(tmp.c64.get(), n, vin, tmp.norms.get() + slot0 + k,
-                                            mode ? tmp.sigma.get() : nullptr, mode,
-                                            tmp.v[(k + 1) & 1].get(), tmp.norms.get() + slot0 + k + 1);
-      OS_CUDA(cudaGetLastError());
+      const float *vin = k == 0 ? tmp.v[2].get() : tmp.v[k & 1].get();
+      const double *nin = k == 0 ? norms : norms + slot0 + k;
+      // The first step follows the staging kernels in plain stream order:
+      // its matrix loads must see them complete.
+      cfg.numAttrs = mode == 0 && k == 0 ? 0 : 1;
+      OS_CUDA(cudaLaunchKernelEx(&cfg, spec_step_kernel, (const float *)tmp.c32.get(), n, tmp.ld, vin, nin,
+                                 (const double *)(norms + R), mode, tmp.v[(k + 1) & 1].get(),
+                                 norms + slot0 + k + 1, mode == 0 && k == 0 ? in.x.get() : (float *)nullptr));
     }
-    return iters & 1;
-  };
-  run(SPEC_RHO_ITERS, 0, 0);
-  spec_sigma_kernel<<<1, 1, 0, s>>>(tmp.norms.get() + SPEC_RHO_ITERS, tmp.sigma.get());
-  OS_CUDA(cudaGetLastError());
-  const int slot = SPEC_RHO_ITERS + 1;
-  OS_CUDA(cudaMemcpyAsync(tmp.norms.get() + slot, tmp.norms.get(), sizeof(double), cudaMemcpyDeviceToDevice, s));
-  const int last = run(SPEC_ITERS, 1, slot);
-  spec_feature_kernel<<<(n + 255) / 256, 256, 0, s>>>(tmp.v[last].get(), tmp.norms.get() + slot + SPEC_ITERS, n,
-                                                      in.x.get(), 4);
+    last = iters & 1;
+  }
+  spec_feature_kernel<<<(n + 255) / 256, 256, 0, s>>>(tmp.v[last].get(), norms + R + SPEC_ITERS, n, in.x.get(),
+                                                      4);
   OS_CUDA(cudaGetLastError());
 }
 

@@ -1,15 +1,16 @@
 // probe.cu -- measured roofline denominators that the driver does not
-// provide: the issue rate of the instructions each exhaustive variant spends
-// per state (three-input add with a constant-bank operand and an integer
-// min; multiply-add and fused add-min; packed 16-bit halves, a three-input
-// add per two states and a three-input per-half min per four), the FP32 FMA
-// rate, and the shared-memory read rate of the dense annealing row update
+// provide: the rate of each exhaustive variant's own inner block walk (the
+// enumeration kernel's instruction sequence without its bookkeeping), the
+// INT32 add + min issue rate, the FP32 FMA rate, and the shared-memory read rate of the dense annealing row update
 // (one 128-bit shared load feeding two paired FP32 FMAs per lane, the
 // instruction pair of a field update).
 #include <cstdint>
 #include <utility>
 
+#include <memory>
+
 #include "common.cuh"
+#include "exhaustive_kernels.cuh"
 
 namespace os {
 namespace probe {
@@ -59,64 +60,42 @@ __global__ void __launch_bounds__(256) int32_probe_kernel(const __grid_constant_
   if (r == 0x7fffffff) P.sink[0] = r;
 }
 
-// The per-state instructions of exhaustive variant V (1: three-input add +
-// min; 2: multiply-add + fused add-min; 3: packed 16-bit halves, one
-// three-input add per two states and one three-input per-half min per four:
-// the packed walk's whole inner loop), STEPS steps of CHAINS independent
-// chains per thread; the step constants come from the parameter bank as in
-// the enumeration kernel.
-struct PairParams {
-  int k[STEPS];
-  int k2s[STEPS];
-  int iters;
-  int *sink;
-};
-
-template <int V, int I>
-__device__ __forceinline__ void pair_step(int (&E)[CHAINS], int (&m)[CHAINS], const int (&c)[CHAINS],
-                                          const PairParams &P, int pos, int neg) {
-#pragma unroll
-  for (int j = 0; j < CHAINS; ++j) {
-    if constexpr (V == 1) {
-      E[j] += P.k[I] + ((I & 1) ? c[j] : -c[j]);
-      m[j] = min(m[j], E[j]);
-    } else if constexpr (V == 2) {
-      E[j] = c[j] * ((I & 1) ? pos : neg) + E[j];
-      m[j] = __viaddmin_s32(E[j], P.k[I], m[j]);
-    } else {
-      const int e1 = E[j];
-      E[j] = E[j] + P.k2s[I] + ((I & 2) ? c[j] : -c[j]);
-      if (I & 1) m[j] = (int)__vimin3_s16x2((unsigned)m[j], (unsigned)e1, (unsigned)E[j]);
-    }
-  }
-}
-
-template <int V, int... Is>
-__device__ __forceinline__ void pair_steps(int (&E)[CHAINS], int (&m)[CHAINS], const int (&c)[CHAINS],
-                                           const PairParams &P, int pos, int neg,
-                                           std::integer_sequence<int, Is...>) {
-  (pair_step<V, Is>(E, m, c, P, pos, neg), ...);
-}
+// The enumeration kernel's own inner block walk for exhaustive variant V
+// (exh::inner_block, MODE 0 or 1, for variants 1 and 2;
+// exh::inner_block_packed for the packed variant 3), one block of 2^G inner
+// steps after another, each from couplings that the previous block's minimum
+// changes -- as in the enumeration, where a walked-bit flip changes them
+// between blocks, so that nothing can be hoisted out of the walk. Full
+// occupancy at the kernel's own launch bounds, no per-item bookkeeping: the
+// ceiling of this variant's instruction sequence. (A walk whose couplings
+// never change lets the compiler move part of the adds to the FMA pipe; the
+// enumeration's cannot, so such a walk is not this kernel's ceiling.)
+constexpr int WALK_G = exh::G_DEFAULT;
 
 template <int V>
-__global__ void __launch_bounds__(256) pair_probe_kernel(const __grid_constant__ PairParams P) {
-  int E[CHAINS], m[CHAINS], c[CHAINS];
-  const int pos = P.k[0] | 1, neg = -pos;  // runtime +-1 (k[0] = 1)
+__global__ void __launch_bounds__(exh::THREADS, 5) walk_probe_kernel(const __grid_constant__ exh::GrayParams<int> P,
+                                                                     int iters, int *sink) {
+  int c[WALK_G];
 #pragma unroll
-  for (int j = 0; j < CHAINS; ++j) {
-    E[j] = threadIdx.x * 7 + j;
-    m[j] = 1 << 30;
-    c[j] = (blockIdx.x + j) & 3;
+  for (int i = 0; i < WALK_G; ++i) c[i] = (int)(((threadIdx.x + blockIdx.x + i) & 3) * (V == 3 ? 65537u : 1u));
+  int E0 = V == 3 ? (int)((16384u + (threadIdx.x & 255)) * 65537u) : (int)threadIdx.x;
+  const int pos = P.one, neg = -P.one;
+  int acc = 0;
+  for (int it = 0; it < iters; ++it) {
+    int m;
+    if constexpr (V == 3) {
+      m = exh::inner_block_packed<WALK_G>(E0, c, P);
+    } else {
+      int E = E0;
+      m = E0;
+      exh::inner_block<int, WALK_G, V - 1>(E, m, c, P, pos, neg);
+    }
+    acc ^= m;
+    E0 += m & 1;
+#pragma unroll
+    for (int i = 0; i < WALK_G; ++i) c[i] += (m >> i) & (V == 3 ? 65537 : 1);
   }
-  for (int it = 0; it < P.iters; ++it) {
-    pair_steps<V>(E, m, c, P, pos, neg, std::make_integer_sequence<int, STEPS>{});
-#pragma unroll
-    for (int j = 0; j < CHAINS; ++j) c[j] ^= m[j] & 1;
-  }
-  int r = 0;
-#pragma unroll
-  for (int j = 0; j < CHAINS; ++j) r ^= m[j] ^ E[j];
-  if (r == 0x7fffffff) P.sink[0] = r;
+  if (acc == 0x7fffffff) sink[0] = acc;
 }
 
 // Per iteration: 8 independent FMA chains x 64 steps.
@@ -217,23 +196,25 @@ os_status os_probe_exhaustive_pair(os_ctx *ctx, int32_t variant, double *states_
     OS_REQUIRE(variant >= 1 && variant <= 3, "variant must be 1, 2 or 3");
     DevBuf<int> sink;
     sink.alloc(1);
-    PairParams P{};
-    for (int i = 0; i < STEPS; ++i) {
-      P.k[i] = i == 0 ? 1 : (int)((i * 2654435761u) & 15);
-      P.k2s[i] = (int)((uint32_t)P.k[i] * 0x10001u);
+    auto P = std::make_unique<exh::GrayParams<int>>();
+    for (int t = 0; t < exh::INNER_MAX; ++t) {
+      P->kf[t] = t == 0 ? 0 : (int)((t * 2654435761u) >> 29) - 4;  // small step deltas in [-4, 3]
+      P->ks[t] = t == 0 ? 0 : P->ks[t - 1] + P->kf[t];
+      P->kp[t] = (int)((uint32_t)P->kf[t] * 65537u);
     }
-    P.iters = 64;
-    P.sink = sink.get();
-    auto kern = variant == 1 ? pair_probe_kernel<1> : variant == 2 ? pair_probe_kernel<2> : pair_probe_kernel<3>;
+    P->one = 1;
+    const int iters = 64;
+    auto kern = variant == 1 ? walk_probe_kernel<1> : variant == 2 ? walk_probe_kernel<2> : walk_probe_kernel<3>;
     int occ = 0;
-    OS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, 256, 0));
+    OS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, exh::THREADS, 0));
     const int grid = ctx->sm_count * (occ > 0 ? occ : 1);
     const double ms = time_ms(ctx->stream, [&] {
-      kern<<<grid, 256, 0, ctx->stream>>>(P);
+      kern<<<grid, exh::THREADS, 0, ctx->stream>>>(*P, iters, sink.get());
       OS_CUDA(cudaGetLastError());
     });
-    const double steps = (double)STEPS * CHAINS * (double)P.iters * grid * 256.0;
-    *states_per_s = steps * (variant == 3 ? 2.0 : 1.0) / (ms * 1e-3);
+    // Per block: 2^G inner states per walk, two walks in the packed variant.
+    const double states = (double)(1 << WALK_G) * (variant == 3 ? 2.0 : 1.0) * iters * grid * exh::THREADS;
+    *states_per_s = states / (ms * 1e-3);
   });
 }
 

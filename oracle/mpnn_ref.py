@@ -37,10 +37,11 @@ def layout(H: int, L: int):
 
 
 def spectral(c: np.ndarray) -> np.ndarray:
-    """Feature u of the GPU's spectral_feature (onesolver_gb300/csrc/mpnn.cu):
+    """Feature u of the GPU's spectral feature (onesolver_gb300/csrc/mpnn.cu):
     power iterations on C^ for its spectral radius rho, then on
-    (1.05 rho I - C^) from the same start vector, in FP64; u = sqrt(n) v
-    sign(v_0)."""
+    (1.05 rho I - C^) from the same start vector; u = sqrt(n) v sign(v_0).
+    Here in FP64; the GPU forms the matrix-vector products in FP32 (FP64
+    norms), which the tests' tolerances on features and predictions cover."""
     n = c.shape[0]
     i = np.arange(n, dtype=np.uint64)
     v0 = 1.0 + 0.25 * (((i * np.uint64(2654435761)) & np.uint64(0xFFFFFFFF)) >> np.uint64(24)).astype(np.float64) / 255.0
