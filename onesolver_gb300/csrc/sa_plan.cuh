@@ -60,6 +60,7 @@ struct os_sa_plan {
   os::DevBuf<double> c64, d64;
   os::DevBuf<unsigned long long> x, xbest;
   os::DevBuf<__nv_bfloat16> bsplit, xmat;   // tensor-core initialisation operands
+  alignas(64) unsigned char init_tmap[2][128];  // TMA tensor maps of xmat and bsplit (CUtensorMap)
 
   // sparse
   int ncolors = 0, nnz = 0, traj_per_cta = 0, deg_max = 1;

@@ -3,7 +3,8 @@
 // MMA issue from shared-memory matrix descriptors with the accumulator in
 // TMEM, completion through an mbarrier, and TMEM -> register loads.
 //
-// Operand layout: no swizzle, K-major "core matrices" of 8 rows x 16 bytes
+// Operand layouts: the 128-byte swizzle of TMA tensor copies
+// (smem_desc_sw128), or no swizzle, K-major "core matrices" of 8 rows x 16 bytes
 // (8 rows x 8 BF16). A tile of R rows x 64 K elements is stored as
 // core matrix (row group i, K group j) at byte offset (i * 8 + j) * 128, row r
 // of it at + 16 r; the descriptors then take LBO = 128 (next core matrix
@@ -49,6 +50,36 @@ __device__ __forceinline__ void fence_proxy_async_smem() {
 __device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
   return (uint64_t)((addr >> 4) & 0x3FFFu) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
          ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
+}
+
+// Descriptor of a K-major operand staged by TMA with the 128-byte swizzle:
+// rows of 128 bytes (64 BF16), 8-row groups 1024 bytes apart (SBO), the
+// leading offset unused; the tile base must be 1024-byte aligned, and a
+// K = 16 step advances the start address by 32 bytes within the row.
+__device__ __forceinline__ uint64_t smem_desc_sw128(uint32_t addr) {
+  return (uint64_t)((addr >> 4) & 0x3FFFu) | (1ull << 16) | ((uint64_t)(1024 >> 4) << 32) | (1ull << 46) |
+         (2ull << 61);
+}
+
+// Cluster helpers: this CTA's rank in its cluster, a full cluster barrier,
+// the cluster-window address of the same shared-memory offset in CTA
+// `rank`, and a 16-byte store to such an address.
+__device__ __forceinline__ uint32_t cluster_ctarank() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+__device__ __forceinline__ void cluster_sync() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+__device__ __forceinline__ uint32_t mapa(uint32_t addr, uint32_t rank) {
+  uint32_t r;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(addr), "r"(rank));
+  return r;
+}
+__device__ __forceinline__ void st_cluster_v4(uint32_t addr, uint32_t a, uint32_t b, uint32_t c, uint32_t d) {
+  asm volatile("st.shared::cluster.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(addr), "r"(a), "r"(b), "r"(c), "r"(d)
+               : "memory");
 }
 
 // Instruction descriptor of kind::f16: FP32 accumulator, BF16 A and B, both

@@ -1,8 +1,9 @@
-// tma.cuh -- bulk async copies (TMA, non-tensor form) and mbarriers, as
-// inline PTX for sm_90+ (used on sm_103a).
+// tma.cuh -- bulk async copies (TMA: the plain bulk form and the tiled
+// tensor form) and mbarriers, as inline PTX for sm_90+ (used on sm_103a).
 //
 // A tile of contiguous rows is moved global -> shared memory by one
-// cp.async.bulk, whose completion is counted in bytes on an mbarrier. Every
+// cp.async.bulk, a box of a 2-D tensor by one cp.async.bulk.tensor; either
+// completion is counted in bytes on an mbarrier. Every
 // wait is bounded: after `limit` failed polls it reports failure instead of
 // spinning forever, and the caller turns that into an error status.
 #ifndef ONESOLVER_TMA_CUH_
@@ -37,6 +38,18 @@ __device__ __forceinline__ void bulk_load(void *dst_smem, const void *src_gmem, 
       "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
           smem_u32(dst_smem)),
       "l"(src_gmem), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+
+// Tiled tensor copy (TMA) of the box at (x, y) -- x the inner coordinate, in
+// elements, whose byte offset must be a multiple of 16 -- from the tensor
+// map `map` (a kernel parameter) to this CTA's shared memory, completing on
+// `bar`.
+__device__ __forceinline__ void tma_load_2d(void *dst_smem, const void *map, int x, int y, uint64_t *bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], "
+      "[%4];" ::"r"(smem_u32(dst_smem)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_u32(bar))
       : "memory");
 }
 
