@@ -17,7 +17,7 @@
 // Output tile: 128 trajectories x 128 sites, its K range (3 ld) split over
 // a cluster of 4 CTAs, one per K quarter, each with its own 128 x 128 FP32
 // accumulator in 128 TMEM columns. K advances in chunks of 64 through a
-// 4-stage ring: one thread issues the chunk's two TMA tensor copies (the
+// 6-stage ring: one thread issues the chunk's two TMA tensor copies (the
 // rows of X and of the split couplings, K-major, 128-byte swizzle) on the
 // stage's `full` mbarrier, another issues four K = 16 MMAs once they have
 // landed and commits them to the stage's `empty` mbarrier, which lets the
@@ -53,7 +53,7 @@ namespace {
 constexpr int IM = 128, IN = 128, IK = 64;  // output tile of the product, K chunk
 constexpr int INIT_CHUNK = 8192;            // trajectories per product (bounds X)
 constexpr uint32_t INIT_WAIT_LIMIT = 1u << 26;
-constexpr int INIT_STAGES = 4, INIT_SPLIT = 4;          // ring depth; CTAs (K quarters) per tile
+constexpr int INIT_STAGES = 6, INIT_SPLIT = 4;          // ring depth; CTAs (K quarters) per tile
 constexpr int INIT_STAGE_BYTES = (IM + IN) * IK * 2;    // A and B chunks of one stage (32 KB)
 constexpr int INIT_RECV_STRIDE = 36;  // floats per received partial row (32 + 4: conflict-free 16-byte stores)
 constexpr int INIT_SMEM = INIT_STAGES * INIT_STAGE_BYTES + 1024;  // + room to align the ring to 1024 bytes
