@@ -164,7 +164,20 @@ os_status os_ctx_create(int32_t device, os_ctx **out) {
                                              cudaDevAttrMultiProcessorCount, device);
     if (err == cudaSuccess)
       err = cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking);
+    if (err == cudaSuccess) {
+      cudaMemPoolProps props = {};
+      props.allocType = cudaMemAllocationTypePinned;
+      props.location.type = cudaMemLocationTypeDevice;
+      props.location.id = device;
+      err = cudaMemPoolCreate(&ctx->pool, &props);
+    }
+    if (err == cudaSuccess) {
+      uint64_t keep = 1ull << 30;
+      err = cudaMemPoolSetAttribute(ctx->pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    }
     if (err != cudaSuccess) {
+      if (ctx->pool) cudaMemPoolDestroy(ctx->pool);
+      if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
       delete ctx;
       throw_error(OS_CUDA_ERROR, "context creation failed: %s", cudaGetErrorString(err));
     }
@@ -177,10 +190,12 @@ os_status os_ctx_destroy(os_ctx *ctx) {
   return guard([&] {
     if (!ctx) return;
     cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     if (ctx->own_stream) {
       cudaStreamSynchronize(ctx->own_stream);
       cudaStreamDestroy(ctx->own_stream);
     }
+    if (ctx->pool) cudaMemPoolDestroy(ctx->pool);
     delete ctx;
   });
 }

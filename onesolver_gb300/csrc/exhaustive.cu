@@ -195,6 +195,7 @@ struct os_exh_plan {
   int launches = 0;
   bool fixed_path_overflow = false;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;  // around the enumeration pass
+  cudaEvent_t ready = nullptr;                // buffers allocated and filled (creation stream)
   DevBuf<int> q32, kf32;
   DevBuf<long long> q64, kf64;
   DevBuf<unsigned char> rec;
@@ -257,10 +258,11 @@ void fill_params(os_exh_plan *p, GrayParams<T> &P, const std::vector<T> &q,
   const int n = p->n;
   std::vector<T> kf(INNER_MAX, 0);
   if (!p->small) inner_constants(q.data(), n, p->G, kf.data());
-  dq.alloc(q.size());
-  OS_CUDA(cudaMemcpy(dq.get(), q.data(), sizeof(T) * q.size(), cudaMemcpyHostToDevice));
-  dkf.alloc(INNER_MAX);
-  OS_CUDA(cudaMemcpy(dkf.get(), kf.data(), sizeof(T) * INNER_MAX, cudaMemcpyHostToDevice));
+  cudaStream_t s = p->ctx->stream;
+  dq.alloc_on(q.size(), p->ctx->pool, s);
+  OS_CUDA(cudaMemcpyAsync(dq.get(), q.data(), sizeof(T) * q.size(), cudaMemcpyHostToDevice, s));
+  dkf.alloc_on(INNER_MAX, p->ctx->pool, s);
+  OS_CUDA(cudaMemcpyAsync(dkf.get(), kf.data(), sizeof(T) * INNER_MAX, cudaMemcpyHostToDevice, s));
   T acc = 0;
   for (int t = 0; t < INNER_MAX; ++t) {
     P.kf[t] = kf[t];
@@ -348,6 +350,7 @@ template <class T> void launch_pass(os_exh_plan *p, GrayParams<T> &P, bool colle
 
 template <class T> void execute_typed(os_exh_plan *p, GrayParams<T> &P) {
   cudaStream_t s = p->ctx->stream;
+  OS_CUDA(cudaStreamWaitEvent(s, p->ready, 0));
   p->launches = 0;
   OS_CUDA(cudaMemsetAsync(p->counters.get() + C_WORK, 0, sizeof(unsigned long long), s));
   OS_CUDA(cudaMemsetAsync(p->counters.get() + C_GBEST, 0x7f, sizeof(unsigned long long), s));
@@ -446,22 +449,30 @@ os_status os_exhaustive_plan_create(os_ctx *ctx, const os_qubo_dense *qubo,
       p->prefix_state = prm.fixed_high_bits ? (prm.prefix << p->free_bits) : 0ull;
       p->user_cap = prm.max_minimisers;
       p->out_cap = std::max<unsigned long long>(prm.max_minimisers, 1ull);
-      p->counters.alloc(C_N);
+      // Plan buffers come stream-ordered from the context's pool, and the
+      // uploads are ordered on the same stream (pageable sources are staged
+      // before the calls return); `ready` marks their end for an execution
+      // on another stream.
+      cudaMemPool_t mp = ctx->pool;
+      cudaStream_t cs = ctx->stream;
+      p->counters.alloc_on(C_N, mp, cs);
       OS_CUDA(cudaEventCreate(&p->ev0));
       OS_CUDA(cudaEventCreate(&p->ev1));
-      p->summary.alloc(1);
-      p->out_states.alloc(p->out_cap);
+      OS_CUDA(cudaEventCreateWithFlags(&p->ready, cudaEventDisableTiming));
+      p->summary.alloc_on(1, mp, cs);
+      p->out_states.alloc_on(p->out_cap, mp, cs);
 
       if (kind == OS_COEF_INT32) {
         std::vector<int> q(f.size());
         for (size_t i = 0; i < f.size(); ++i) q[i] = (int)f[i];
         // Record buffers sized after the grid is known.
-        p->rec.alloc(sizeof(CtaRecord<int>) * 1);
+        p->rec.alloc_on(sizeof(CtaRecord<int>) * 1, mp, cs);
         fill_params(p, p->p32, q, p->q32, p->kf32);
         p->ctas = grid_for(p, p->p32);
-        p->rec.alloc(sizeof(CtaRecord<int>) * p->ctas);
-        p->cta_states.alloc((size_t)p->ctas * CTA_CAP);
-        fill_params(p, p->p32, q, p->q32, p->kf32);
+        p->rec.alloc_on(sizeof(CtaRecord<int>) * p->ctas, mp, cs);
+        p->cta_states.alloc_on((size_t)p->ctas * CTA_CAP, mp, cs);
+        p->p32.cta = reinterpret_cast<CtaRecord<int> *>(p->rec.get());  // records sized for the grid
+        p->p32.cta_states = p->cta_states.get();
       } else {
         std::vector<long long> q(f.size());
         if (kind == OS_COEF_INT64) {
@@ -476,18 +487,20 @@ os_status os_exhaustive_plan_create(os_ctx *ctx, const os_qubo_dense *qubo,
           for (size_t i = 0; i < f.size(); ++i) q[i] = std::llround(f[i] * S);
           const double delta = P * 1.2e-16 * abs_sum;  // bound on the FP64 reference error
           p->window = (long long)std::ceil(P + 2.0 * S * delta) + 2;
-          p->d_f.alloc(f.size());
-          OS_CUDA(cudaMemcpy(p->d_f.get(), f.data(), sizeof(double) * f.size(), cudaMemcpyHostToDevice));
-          p->cand.alloc(CAND_CAP);
-          p->cand_e.alloc(CAND_CAP);
+          p->d_f.alloc_on(f.size(), mp, cs);
+          OS_CUDA(cudaMemcpyAsync(p->d_f.get(), f.data(), sizeof(double) * f.size(), cudaMemcpyHostToDevice, cs));
+          p->cand.alloc_on(CAND_CAP, mp, cs);
+          p->cand_e.alloc_on(CAND_CAP, mp, cs);
         }
-        p->rec.alloc(sizeof(CtaRecord<long long>) * 1);
+        p->rec.alloc_on(sizeof(CtaRecord<long long>) * 1, mp, cs);
         fill_params(p, p->p64, q, p->q64, p->kf64);
         p->ctas = grid_for(p, p->p64);
-        p->rec.alloc(sizeof(CtaRecord<long long>) * p->ctas);
-        p->cta_states.alloc((size_t)p->ctas * CTA_CAP);
-        fill_params(p, p->p64, q, p->q64, p->kf64);
+        p->rec.alloc_on(sizeof(CtaRecord<long long>) * p->ctas, mp, cs);
+        p->cta_states.alloc_on((size_t)p->ctas * CTA_CAP, mp, cs);
+        p->p64.cta = reinterpret_cast<CtaRecord<long long> *>(p->rec.get());  // records sized for the grid
+        p->p64.cta_states = p->cta_states.get();
       }
+      OS_CUDA(cudaEventRecord(p->ready, cs));
     } catch (...) {
       delete p;
       throw;
@@ -592,6 +605,7 @@ void os_exhaustive_plan_destroy(os_exh_plan *p) {
   cudaStreamSynchronize(p->ctx->stream);
   if (p->ev0) cudaEventDestroy(p->ev0);
   if (p->ev1) cudaEventDestroy(p->ev1);
+  if (p->ready) cudaEventDestroy(p->ready);
   delete p;
 }
 

@@ -208,15 +208,18 @@ void plan_create_dense(os_sa_plan *p, const os_qubo_dense *q) {
   p->slot_cls = slot_class(hst.nslots);
   const size_t T = p->T;
   const size_t ld = hst.ld;
-  p->c32.alloc(ld * ld);
-  p->d32.alloc(ld);
-  p->c64.alloc(ld * ld);
-  p->d64.alloc(ld);
-  p->f.alloc((size_t)hst.n * hst.n);
+  // The plan's device buffers come stream-ordered from the context's pool
+  // (freed in order at destruction, the blocks kept for the next plan).
   cudaStream_t s = p->ctx->stream;
+  cudaMemPool_t mp = p->ctx->pool;
+  p->c32.alloc_on(ld * ld, mp, s);
+  p->d32.alloc_on(ld, mp, s);
+  p->c64.alloc_on(ld * ld, mp, s);
+  p->d64.alloc_on(ld, mp, s);
+  p->f.alloc_on((size_t)hst.n * hst.n, mp, s);
   OS_CUDA(cudaMemcpyAsync(p->f.get(), q->f, sizeof(double) * hst.n * hst.n, cudaMemcpyHostToDevice, s));
   DevBuf<int> bad;
-  bad.alloc(1);
+  bad.alloc_on(1, mp, s);
   OS_CUDA(cudaMemsetAsync(bad.get(), 0, sizeof(int), s));
   stage_dense_kernel<<<(unsigned)((ld + 7) / 8), 256, 0, s>>>(p->f.get(), hst.n, hst.ld, p->c32.get(), p->c64.get(),
                                                              p->d32.get(), p->d64.get(), bad.get());
@@ -225,18 +228,21 @@ void plan_create_dense(os_sa_plan *p, const os_qubo_dense *q) {
   OS_CUDA(cudaMemcpyAsync(&nbad, bad.get(), sizeof(int), cudaMemcpyDeviceToHost, s));
   OS_CUDA(cudaStreamSynchronize(s));
   OS_REQUIRE(nbad == 0, "the QUBO has %d non-finite coefficients", nbad);
-  p->h.alloc(T * hst.nslots * 32);
+  p->h.alloc_on(T * hst.nslots * 32, mp, s);
   dense_init_prepare(p, s);
-  p->x.alloc(T * 32);
-  p->xbest.alloc(T * 32);
-  p->e.alloc(T);
-  p->ebest.alloc(T);
-  p->accepted.alloc(T);
-  p->states.alloc(T * (size_t)hst.n);
-  p->e64.alloc(T);
+  p->x.alloc_on(T * 32, mp, s);
+  p->xbest.alloc_on(T * 32, mp, s);
+  p->e.alloc_on(T, mp, s);
+  p->ebest.alloc_on(T, mp, s);
+  p->accepted.alloc_on(T, mp, s);
+  p->states.alloc_on(T * (size_t)hst.n, mp, s);
+  p->e64.alloc_on(T, mp, s);
   p->tiled = p->sequential && hst.ld <= TILE_MAX_LD;
   p->warps = dense_warps((int)T, p->ctx->sm_count, p->tiled);
-  p->status.alloc(1);
+  p->status.alloc_on(1, mp, s);
+  OS_CUDA(cudaMemsetAsync(p->status.get(), 0, sizeof(int), s));
+  if (!p->ready) OS_CUDA(cudaEventCreateWithFlags(&p->ready, cudaEventDisableTiming));
+  OS_CUDA(cudaEventRecord(p->ready, s));  // an execution on another stream waits for it
 }
 
 ResyncArgs dense_resync_args(os_sa_plan *p, int init) {
@@ -483,6 +489,7 @@ os_status os_sa_plan_execute(os_sa_plan *p) {
   return guard([&] {
     OS_REQUIRE(p != nullptr, "null plan");
     activate(p->ctx);
+    if (p->ready) OS_CUDA(cudaStreamWaitEvent(p->ctx->stream, p->ready, 0));
     if (p->kind == 0)
       execute_dense(p);
     else if (p->kind == 1)
@@ -514,6 +521,7 @@ void os_sa_plan_destroy(os_sa_plan *p) {
   cudaSetDevice(p->ctx->device);
   cudaStreamSynchronize(p->ctx->stream);
   release_batch(p);
+  if (p->ready) cudaEventDestroy(p->ready);
   delete p;
 }
 

@@ -288,12 +288,12 @@ void dense_init_prepare(os_sa_plan *p, cudaStream_t s) {
   static_assert(sizeof(CUtensorMap) == sizeof(p->init_tmap[0]), "tensor map size");
   OS_CUDA(cudaFuncSetAttribute(init_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, INIT_SMEM));
   const size_t nn = (size_t)p->ld * p->ld;
-  p->bsplit.alloc(3 * nn);
+  p->bsplit.alloc_on(3 * nn, p->ctx->pool, s);
   split_kernel<<<(unsigned)ceil_div_u64(nn, 256), 256, 0, s>>>(p->c64.get(), p->ld, p->bsplit.get());
   OS_CUDA(cudaGetLastError());
   const int rows = std::min(p->T, INIT_CHUNK);
   const size_t xrows = (size_t)(rows + IM - 1) / IM * IM;
-  p->xmat.alloc(xrows * p->ld);
+  p->xmat.alloc_on(xrows * p->ld, p->ctx->pool, s);
   encode_bf16_map(p->init_tmap[0], p->xmat.get(), xrows, (uint64_t)p->ld);
   encode_bf16_map(p->init_tmap[1], p->bsplit.get(), (uint64_t)p->ld, 3 * (uint64_t)p->ld);
 }

@@ -64,6 +64,7 @@ struct os_sa_plan {
 
   // sparse
   int ncolors = 0, nnz = 0, traj_per_cta = 0, deg_max = 1;
+  cudaEvent_t ready = nullptr;  // dense plans: buffers allocated and filled (creation stream)
   os::DevBuf<int> row_ptr, col, color_sites, color_ptr;
   os::DevBuf<int2> ell;                     // padded neighbour table (site, coupling bits)
   os::DevBuf<float> val32, diag32;
