@@ -152,6 +152,20 @@ def test_training_learns_and_warm_start_gains(native, orc, ctx):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("n", [1024, 1100])
+def test_prediction_at_and_past_the_register_row_matches_oracle(native, ctx, n):
+    """The FP32 power iteration (rows of 1,024 and of 1,152 padded
+    couplings, past the 1,024 the staged row loads cover in registers) and
+    the whole forward pass match the oracle's FP64 restatement."""
+    net = native.WarmStartNet(seed=5, ctx=ctx)
+    f = random_normal_qubo(n, 11)
+    p = net.predict(f)
+    _, _, p_ref = mpnn_ref.loss_grad(net.params().astype(np.float64), f, np.zeros(n))
+    np.testing.assert_allclose(p, p_ref, atol=5e-3)
+    net.close()
+
+
+@pytest.mark.gpu
 def test_predict_graph_matches_oracle_and_follows_parameters(native, ctx):
     """predict() replays one captured graph per size: its probabilities match
     the oracle's forward pass, repeat exactly, follow a size change and read
