@@ -44,7 +44,7 @@ typedef enum os_status {
   OS_OVERFLOW_MINIMISERS = 4,  /* more minimisers than the caller's buffer holds */
   OS_NO_DEVICE = 5,            /* no CUDA device of the requested index */
   OS_PARSE_ERROR = 6,          /* .qubo text rejected (qubo.hpp:313-314,355-373,413-415) */
-  OS_UNSUPPORTED = 7           /* e.g. --device-type host/cpu: this build has no CPU backend */
+  OS_UNSUPPORTED = 7           /* e.g. --device-type host/cpu: this library has no CPU backend */
 } os_status;
 
 /* ------------------------------------------------------------------------ */
@@ -63,7 +63,7 @@ const char *os_status_string(os_status status);
 
 /* Device selection by the reference's --device-type string. Replaces
  * devices::construct_device_selector (include/helpers/devices.hpp:27-42):
- * "gpu" -> CUDA device 0; "cpu" and "host" -> OS_UNSUPPORTED (this build
+ * "gpu" -> CUDA device 0; "cpu" and "host" -> OS_UNSUPPORTED (this library
  * has no CPU backend and never falls back to one); anything else ->
  * OS_INVALID_ARG with "Unknown device type: <s>". */
 os_status os_select_device(const char *device_type, int32_t *device_out);

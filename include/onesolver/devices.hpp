@@ -59,7 +59,7 @@ struct device_selector {
 using device_selector_ptr = std::unique_ptr<device_selector>;
 
 // construct_device_selector (devices.hpp:27-42): "gpu" -> CUDA device 0;
-// "cpu"/"host" -> std::runtime_error (no CPU backend in this build); any
+// "cpu"/"host" -> std::runtime_error (no CPU backend in this library); any
 // other string -> std::invalid_argument("Unknown device type: ...").
 inline device_selector_ptr construct_device_selector(std::string device_type) {
   int dev = -1;

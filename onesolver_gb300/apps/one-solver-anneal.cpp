@@ -3,7 +3,7 @@
 // Same flags, defaults, messages and exit codes as the reference's
 // app/one-solver-anneal.cpp (options :55-72, validation :83-115, echo
 // :117-127, schedules :153-161, run and save :163-170, errors :171-176),
-// with --device-type gpu (the default here: this build has no host/cpu
+// with --device-type gpu (the default here: this library has no host/cpu
 // backend) and additive options for the new solver features.
 #include <fstream>
 #include <iostream>

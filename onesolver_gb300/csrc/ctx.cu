@@ -132,7 +132,7 @@ os_status os_select_device(const char *device_type, int32_t *device_out) {
       *device_out = 0;
     } else if (t == "cpu" || t == "host") {
       throw_error(OS_UNSUPPORTED,
-                  "Device type %s is not available: this build runs on the GPU "
+                  "Device type %s is not available: this library runs on the GPU "
                   "only (use --device-type gpu).",
                   device_type);
     } else {

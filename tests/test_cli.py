@@ -85,7 +85,7 @@ def test_device_types(apps, which, small_input, tmp_path):
     _, path = small_input
     rc, _, err = run(exe, "--input", path, "--output", tmp_path / "o.csv", "--device-type", "fpga")
     assert rc == 255 and "Unknown device type: fpga" in err
-    # host and cpu are valid names without a backend in this build
+    # host and cpu are valid names without a backend in this library
     for dev in ("host", "cpu"):
         rc, _, err = run(exe, "--input", path, "--output", tmp_path / "o.csv", "--device-type", dev)
         assert rc == 1 and "No devices of given type could be initialized." in err

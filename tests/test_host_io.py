@@ -114,7 +114,7 @@ def test_load_file(native, tmp_path, golden_exhaustive):
 
 
 def test_device_selector_strings(native):
-    # devices_test.cpp: host/cpu/gpu are the accepted strings; this build has
+    # devices_test.cpp: host/cpu/gpu are the accepted strings; this library has
     # no CPU backend, so host/cpu are refused with UNSUPPORTED.
     for t in ("host", "cpu"):
         with pytest.raises(native.OneSolverError) as e:
