@@ -227,8 +227,7 @@ void os_exhaustive_plan_destroy(os_exh_plan *plan);
  *     requests return OS_INVALID_ARG. inner_bits and variant are checked and
  *     honoured as os_exhaustive_run does.
  *   - The first call on a device looks up the array's device address
- *     (cudaGetSymbolAddress), so it belongs before any stream capture on
- *     that device.
+ *     (cudaGetSymbolAddress) and keeps it for later calls.
  *   - Every call copies the answer back into the caller's host buffers and
  *     waits on `stream` for that before it returns.
  *   - Every call reuses the same array, so calls whose work overlaps on the
