@@ -106,7 +106,7 @@ def test_returned_states_rescore(native, orc, ctx, n, site_order, acceptance):
     assert res.attempts == 50 * steps
 
 
-@pytest.mark.parametrize("n,T", [(200, 37), (1024, 130)])
+@pytest.mark.parametrize("n,T", [(100, 300), (200, 37), (1024, 130)])
 def test_integer_instance_has_zero_field_drift(native, orc, ctx, n, T):
     """Integer couplings: the tensor-core initial fields (three BF16 terms,
     FP32 accumulation) and every FP32 field update are exact, so the FP64
