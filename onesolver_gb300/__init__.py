@@ -24,6 +24,7 @@ from __future__ import annotations
 import ctypes as C
 import math
 import os
+import weakref
 from dataclasses import dataclass, field
 from pathlib import Path
 from typing import Optional, Sequence
@@ -261,8 +262,14 @@ class Context:
 
     def __init__(self, device: int = 0):
         self._h = _P()
+        self._children = weakref.WeakSet()
         _check(lib().os_ctx_create(device, C.byref(self._h)))
         self.device = device
+
+    def _adopt(self, obj) -> None:
+        """Plans and networks made on this context: close() closes them
+        first (their device buffers are freed in order on its stream)."""
+        self._children.add(obj)
 
     @property
     def handle(self):
@@ -273,6 +280,11 @@ class Context:
 
     def close(self) -> None:
         if self._h:
+            for child in list(self._children):
+                try:
+                    child.close()
+                except Exception:
+                    pass
             lib().os_ctx_destroy(self._h)
             self._h = _P()
 
@@ -465,6 +477,7 @@ class ExhaustivePlan:
                  fixed_high_bits: int = 0, prefix: int = 0, max_minimisers: int = 4096, inner_bits: int = 0,
                  variant: int = 0):
         self.ctx = ctx or default_context()
+        self.ctx._adopt(self)
         q, self._keep = _dense(f)
         self.cap = max_minimisers
         self._h = _P()
@@ -710,6 +723,7 @@ class AnnealPlan(_PlanReplay):
                  seed: int = 1234, acceptance: int = ACCEPT_PHYSICAL, site_order: int = SITES_SEQUENTIAL,
                  resync_every: int = 0, init_prob: Optional[np.ndarray] = None, ctx: Optional[Context] = None):
         self.ctx = ctx or default_context()
+        self.ctx._adopt(self)
         self.T = num_tries
         self._b = np.ascontiguousarray(beta, dtype=np.float64)
         self._ip = None if init_prob is None else np.ascontiguousarray(init_prob, dtype=np.float32)
@@ -935,6 +949,7 @@ class BatchedAnnealPlan(_PlanReplay):
                  seed: int = 1234, acceptance: int = ACCEPT_PHYSICAL, resync_every: int = 0,
                  ctx: Optional[Context] = None):
         self.ctx = ctx or default_context()
+        self.ctx._adopt(self)
         self.T = num_tries
         self._arr, self._fs = _batch_inputs(instances)
         self._b = np.ascontiguousarray(beta, dtype=np.float64)
@@ -1037,6 +1052,7 @@ class WarmStartNet:
     def __init__(self, *, hidden: int = 64, layers: int = 3, orient: bool = True, seed: int = 1,
                  ctx: Optional[Context] = None):
         self.ctx = ctx or default_context()
+        self.ctx._adopt(self)
         self._h = _P()
         self.orient = orient
         _check(lib().os_mpnn_create(self.ctx.handle, hidden, layers, int(orient), seed, C.byref(self._h)))
