@@ -287,8 +287,8 @@ void plan_create_batched(os_sa_plan *p, int num, const os_qubo_dense *qs) {
   p->e64.alloc(traj);
   p->status.alloc(1);
   B->work.alloc(1);
-  int max_ld = *std::max_element(B->ld.begin(), B->ld.end());
-  B->smem = (size_t)2 * TILE_ROWS * max_ld * sizeof(float);
+  B->smem = 0;
+  for (int ldk : B->ld) B->smem = std::max(B->smem, tile_smem_bytes(ldk));
   OS_BATCH_DISPATCH(p->slot_cls, set_batch_smem, B->smem);
   OS_CUDA(cudaMemset(p->status.get(), 0, sizeof(int)));
   p->warps = autotune_warps(p, *B);
