@@ -32,21 +32,6 @@ namespace sa {
 constexpr int BATCH_MAX_LD = 1792;     // two 16-row FP32 tiles in shared memory
 constexpr int BATCH_PROBE_STEPS = 4;
 
-template <int SLOTS> void launch_batch_tile(const BatchArgs &b, int grid, size_t smem, cudaStream_t s) {
-  sa_batch_tile_kernel<SLOTS><<<grid, b.W * 32, smem, s>>>(b);
-}
-template <int SLOTS> void set_batch_smem(size_t smem) {
-  OS_CUDA(cudaFuncSetAttribute(sa_batch_tile_kernel<SLOTS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               (int)smem));
-}
-template <int SLOTS> void batch_max_threads(int *out) {
-  cudaFuncAttributes attr;
-  OS_CUDA(cudaFuncGetAttributes(&attr, sa_batch_tile_kernel<SLOTS>));
-  *out = attr.maxThreadsPerBlock;
-}
-template <int SLOTS> void batch_occupancy(int W, size_t smem, int *occ) {
-  OS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(occ, sa_batch_tile_kernel<SLOTS>, W * 32, smem));
-}
 template <int SLOTS> void launch_batch_resync(const BatchResyncArgs &b, cudaStream_t s) {
   const int warps = 4;
   const unsigned grid = (unsigned)ceil_div_u64((unsigned long long)b.total, warps);
@@ -147,7 +132,7 @@ BatchResyncArgs resync_args(os_sa_plan *p, BatchState &B, int init) {
 
 int batch_grid(os_sa_plan *p, BatchState &B, int W) {
   int occ = 0;
-  OS_BATCH_DISPATCH(p->slot_cls, batch_occupancy, W, B.smem, &occ);
+  batch_tile_occupancy(p->slot_cls, W, B.smem, &occ);
   if (occ < 1) occ = 1;
   return std::max(1, std::min(B.num_items, p->ctx->sm_count * occ));
 }
@@ -156,7 +141,7 @@ int batch_grid(os_sa_plan *p, BatchState &B, int W) {
 int autotune_warps(os_sa_plan *p, BatchState &B) {
   cudaStream_t s = p->ctx->stream;
   int max_threads = 0;
-  OS_BATCH_DISPATCH(p->slot_cls, batch_max_threads, &max_threads);
+  batch_tile_max_threads(p->slot_cls, &max_threads);
   BatchResyncArgs r = resync_args(p, B, 1);
   OS_BATCH_DISPATCH(p->slot_cls, launch_batch_resync, r, s);
   OS_CUDA(cudaGetLastError());
@@ -173,7 +158,7 @@ int autotune_warps(os_sa_plan *p, BatchState &B) {
     OS_CUDA(cudaMemsetAsync(B.work.get(), 0, sizeof(unsigned), s));
     BatchArgs a = batch_args(p, B, W, 0, probe);
     OS_CUDA(cudaEventRecord(e0, s));
-    OS_BATCH_DISPATCH(p->slot_cls, launch_batch_tile, a, grid, B.smem, s);
+    batch_tile_launch(a, p->slot_cls, grid, B.smem, s);
     OS_CUDA(cudaGetLastError());
     OS_CUDA(cudaEventRecord(e1, s));
     OS_CUDA(cudaEventSynchronize(e1));
@@ -289,7 +274,7 @@ void plan_create_batched(os_sa_plan *p, int num, const os_qubo_dense *qs) {
   B->work.alloc(1);
   B->smem = 0;
   for (int ldk : B->ld) B->smem = std::max(B->smem, tile_smem_bytes(ldk));
-  OS_BATCH_DISPATCH(p->slot_cls, set_batch_smem, B->smem);
+  batch_tile_set_smem(p->slot_cls, B->smem);
   OS_CUDA(cudaMemset(p->status.get(), 0, sizeof(int)));
   p->warps = autotune_warps(p, *B);
   build_items(p, *B, p->warps);
@@ -319,7 +304,7 @@ void enqueue_batched(os_sa_plan *p, BatchState &B, cudaStream_t s) {
     if (p->replay)
       batch_tile_replay(a, p->slot_cls, B.grid, B.smem, s);
     else
-      OS_BATCH_DISPATCH(p->slot_cls, launch_batch_tile, a, B.grid, B.smem, s);
+      batch_tile_launch(a, p->slot_cls, B.grid, B.smem, s);
     OS_CUDA(cudaGetLastError());
     OS_CUDA(cudaEventRecordWithFlags(p->event(2 * chunk + 1), s, cudaEventRecordExternal));
     OS_BATCH_DISPATCH(p->slot_cls, launch_batch_resync, r, s);

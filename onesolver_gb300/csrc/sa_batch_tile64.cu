@@ -1,0 +1,12 @@
+// sa_batch_tile64.cu -- the production batched sweep kernel's 64-slot class
+// (rows up to 2,048 sites), the slowest to compile, in a translation unit of
+// its own (see sa_batch_tile.cuh).
+#include "sa_batch_tile.cuh"
+
+namespace os {
+namespace sa {
+
+template void batch_tile_op<64, false>(BatchTileOp, const BatchArgs *, int, int, size_t, cudaStream_t, int *);
+
+}  // namespace sa
+}  // namespace os

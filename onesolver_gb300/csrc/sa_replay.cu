@@ -17,10 +17,10 @@
 // kernels: exp((E - E') / beta) > u is dE < -beta ln u and
 // exp(-beta dE) > u is dE < -ln(u) / beta.
 //
-// This file holds the dense and batched REPLAY instantiations (their own
-// translation unit, compiled beside the production kernels) and the entry
-// points os_sa_plan_set_replay, os_sa_plan_trajectories and
-// os_sa_plan_sweep_order.
+// This file holds the dense REPLAY instantiations (their own translation
+// unit, compiled beside the production kernels; the batched ones are in
+// sa_replay_batch.cu) and the entry points os_sa_plan_set_replay,
+// os_sa_plan_trajectories and os_sa_plan_sweep_order.
 #include <cstring>
 #include <vector>
 
@@ -49,13 +49,6 @@ template <int SLOTS> void replay_seq(const DenseArgs &a, int warps, cudaStream_t
 template <int SLOTS> void replay_rand(const DenseArgs &a, int warps, cudaStream_t s) {
   const int grid = (a.traj_count + warps - 1) / warps;
   sa_dense_rand_kernel<SLOTS, true><<<grid, warps * 32, 0, s>>>(a);
-}
-template <int SLOTS> void replay_batch(const BatchArgs &b, int grid, size_t smem, cudaStream_t s) {
-  sa_batch_tile_kernel<SLOTS, true><<<grid, b.W * 32, smem, s>>>(b);
-}
-template <int SLOTS> void replay_batch_smem(size_t smem) {
-  OS_CUDA(cudaFuncSetAttribute(sa_batch_tile_kernel<SLOTS, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               (int)smem));
 }
 
 #define OS_REPLAY_DISPATCH(cls, fn, ...)                                \
@@ -86,12 +79,6 @@ void dense_sweeps_replay(const DenseArgs &a, int slot_cls, int warps, bool seque
   OS_CUDA(cudaGetLastError());
 }
 
-void batch_tile_replay(const BatchArgs &b, int slot_cls, int grid, size_t smem, cudaStream_t s) {
-  OS_REPLAY_DISPATCH(slot_cls, replay_batch, b, grid, smem, s);
-  OS_CUDA(cudaGetLastError());
-}
-
-void batch_replay_smem(int slot_cls, size_t smem) { OS_REPLAY_DISPATCH(slot_cls, replay_batch_smem, smem); }
 
 }  // namespace sa
 }  // namespace os
