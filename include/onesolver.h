@@ -599,8 +599,8 @@ os_status os_mpnn_predict(os_mpnn *model, const os_qubo_dense *qubo, float *prob
 os_status os_sa_plan_warm_start(os_sa_plan *plan, os_mpnn *model);
 
 /* Measured roofline denominators for the integer/FP32/shared-memory-bound
- * paths (the measured peaks cover HBM copy bandwidth and bf16 GEMMs
- * only): the INT32 issue rate of the enumeration's per-state instruction pair
+ * paths (the pool-wide measured peaks cover HBM copy bandwidth and bf16
+ * GEMMs only): the INT32 issue rate of the enumeration's per-state instruction pair
  * (three-input add, integer min), in Gop/s; the FP32 FMA rate, in GFLOP/s;
  * and the shared-memory read rate of the annealing field update (128-bit
  * shared loads feeding paired FP32 FMAs), in GB/s. No reference counterpart. */

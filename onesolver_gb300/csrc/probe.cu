@@ -1,5 +1,5 @@
-// probe.cu -- measured roofline denominators that the driver does not
-// provide: the rate of each exhaustive variant's own inner block walk (the
+// probe.cu -- measured roofline denominators beyond the HBM copy and bf16
+// GEMM peaks: the rate of each exhaustive variant's own inner block walk (the
 // enumeration kernel's instruction sequence without its bookkeeping), the
 // INT32 add + min issue rate, the FP32 FMA rate, and the shared-memory read rate of the dense annealing row update
 // (one 128-bit shared load feeding two paired FP32 FMAs per lane, the

@@ -3,8 +3,8 @@
 Exhaustive search shards the state space by its top bits over the ranks and
 merges one record per rank on rank 0; the bench's N > 1 timing takes the
 maximum over ranks. The shard solver here is the oracle (exhaustive::solve
-restated), so the host logic is checked without a GPU; on a GPU machine the same
-function runs `gpu_shard_solver`.
+restated), so the host logic is checked without a GPU; on a GPU machine the
+same function runs `gpu_shard_solver`.
 """
 from __future__ import annotations
 
