@@ -74,7 +74,11 @@ os_status os_device_name(int32_t device, char *buf, size_t cap);
 
 /* Execution context: one CUDA device, one stream, cached device buffers.
  * Replaces the sycl::queue the reference passes to its solvers
- * (app/one-solver-anneal.cpp:139-147). */
+ * (app/one-solver-anneal.cpp:139-147).
+ * Every plan and network made on a context must be destroyed before the
+ * context: their device buffers come from the context's stream-ordered
+ * memory pool and are returned on its stream. os_ctx_destroy waits for the
+ * context's stream before it releases the stream and the pool. */
 typedef struct os_ctx os_ctx;
 os_status os_ctx_create(int32_t device, os_ctx **out);
 os_status os_ctx_destroy(os_ctx *ctx);
