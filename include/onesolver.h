@@ -83,7 +83,11 @@ typedef struct os_ctx os_ctx;
 os_status os_ctx_create(int32_t device, os_ctx **out);
 os_status os_ctx_destroy(os_ctx *ctx);
 /* Use a caller-owned cudaStream_t (passed as void*) instead of the
- * context's own stream; NULL restores the context's stream. */
+ * context's own stream; NULL restores the context's stream. A plan's
+ * destroy waits for the stream current at that moment and returns the
+ * plan's buffers on the stream it was created on: a caller that executed a
+ * plan on another stream waits for that stream (or makes it current again)
+ * before destroying the plan. */
 os_status os_ctx_set_stream(os_ctx *ctx, void *stream);
 
 /* ------------------------------------------------------------------------ */
