@@ -102,6 +102,7 @@ __global__ void __launch_bounds__(128) gemm_ch_kernel(const __nv_bfloat16 *__res
   constexpr uint32_t idesc = tc05::idesc_bf16_f32(TM, GN);
   const int nchunks = ks / TK;
   bool bad = false;
+  int committed = 0;  // chunks whose MMAs were issued and committed
   for (int c = 0; c < nchunks; ++c) {
     const int b = c & 1;
     if (c >= 2) {  // the MMAs of chunk c - 2 have released buffer b
@@ -135,11 +136,18 @@ __global__ void __launch_bounds__(128) gemm_ch_kernel(const __nv_bfloat16 *__res
       }
       tc05::commit(&bar[b]);
     }
+    committed = c + 1;
   }
   if (!bad) {  // the last commit covers every MMA issued before it
     const int c = nchunks - 1;
     const bool ok = mbar_wait_bounded(&bar[c & 1], (uint32_t)((c >> 1) & 1), TC_WAIT_LIMIT);
     bad = __syncthreads_or(!ok);
+  }
+  if (bad && tid == 0 && committed > 0) {
+    // Let MMAs still in flight finish (bounded) before the accumulator is
+    // freed; the last commit covers all of them.
+    const int c = committed - 1;
+    mbar_wait_bounded(&bar[c & 1], (uint32_t)((c >> 1) & 1), TC_WAIT_LIMIT);
   }
   tc05::fence_after_sync();
   if (!bad) {

@@ -148,6 +148,7 @@ __global__ void __cluster_dims__(1, 1, INIT_SPLIT) __launch_bounds__(128, 1)
   constexpr uint32_t idesc = tc05::idesc_bf16_f32(IM, IN);
   bool bad = false;
   if (warp == 0 && lane == 0) {  // copies
+    int issued = 0;
     for (int c = c_begin; c < c_end; ++c) {
       const int i = c - c_begin, s = i % INIT_STAGES, u = i / INIT_STAGES;
       if (u > 0 && !mbar_wait_bounded(&empty[s], (uint32_t)((u - 1) & 1), INIT_WAIT_LIMIT)) {
@@ -158,6 +159,15 @@ __global__ void __cluster_dims__(1, 1, INIT_SPLIT) __launch_bounds__(128, 1)
       const int k0 = c * IK;
       tma_load_2d(sA(s), &tmx, k0 % ld, row0, &full[s]);
       tma_load_2d(sB(s), &tmb, k0, col0, &full[s]);
+      issued = i + 1;
+    }
+    // Let the copies land (bounded) before the CTA goes on to reuse the ring
+    // or exit: after a failure the MMA thread may have stopped consuming
+    // them. A stage is reloaded only after the MMAs released its previous
+    // copy, so only its last copy can be pending.
+    for (int s = 0; s < INIT_STAGES && s < issued; ++s) {
+      const int last = s + ((issued - 1 - s) / INIT_STAGES) * INIT_STAGES;
+      if (!mbar_wait_bounded(&full[s], (uint32_t)((last / INIT_STAGES) & 1), INIT_WAIT_LIMIT)) bad = true;
     }
   } else if (warp == 1 && lane == 0) {  // MMAs
     for (int c = c_begin; c < c_end; ++c) {

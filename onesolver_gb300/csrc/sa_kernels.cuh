@@ -412,9 +412,13 @@ __device__ __forceinline__ bool tile_item_impl(const DenseArgs &a, float *tiles,
         }
         // Every warp is done with this buffer; refill it with tile g + 2.
         if (__syncthreads_or(!ok)) {
-          // Let copies still in flight land (bounded) before returning.
+          // Let copies still in flight land (bounded) before returning: the
+          // phases of tile g (whose wait ran out; its parity bit is already
+          // flipped) and of tile g + 1 (when the run has it; else the wait
+          // just runs out).
           if (threadIdx.x == 0) {
-            for (int b2 = 0; b2 < 2; ++b2) mbar_wait_bounded(&bar[b2], parity[b2], TILE_WAIT_LIMIT);
+            for (int b2 = 0; b2 < 2; ++b2)
+              mbar_wait_bounded(&bar[b2], parity[b2] ^ (b2 == half ? 1u : 0u), TILE_WAIT_LIMIT);
             if (a.status) atomicExch(a.status, 1);
           }
           return false;
@@ -488,9 +492,10 @@ __host__ __device__ __forceinline__ size_t tile_smem_bytes(int ld) {
 }
 // Shared state of the tile pipeline.
 struct TileSync {
-  uint64_t full[TILE_MAX_BUFS];  // a buffer's copy has landed (transaction bytes)
-  unsigned done[TILE_MAX_BUFS];  // warps done with a buffer's current tile
-  int fail;                      // a bounded wait ran out
+  uint64_t full[TILE_MAX_BUFS];    // a buffer's copy has landed (transaction bytes)
+  unsigned done[TILE_MAX_BUFS];    // warps done with a buffer's current tile
+  unsigned issued[TILE_MAX_BUFS];  // copies issued into a buffer since launch (one phase each)
+  int fail;                        // a bounded wait ran out
 };
 
 // Wait for buffer b's copy of the given phase; false once any warp's wait has
@@ -548,6 +553,7 @@ __device__ __forceinline__ bool batch_tile_item_impl(const DenseArgs &a, float *
   // Tile g (half-slot g mod halves of the run) goes to buffer g mod NB.
   auto issue = [&](long long g, int b) {
     const int hs = (int)(g % halves);
+    ++ts->issued[b];
     mbar_arrive_expect_tx(&ts->full[b], tile_bytes);
     bulk_load(tiles + (size_t)b * tile_floats, a.c + (size_t)hs * TILE_ROWS * ld, tile_bytes, &ts->full[b]);
   };
@@ -622,9 +628,14 @@ __device__ __forceinline__ bool batch_tile_item_impl(const DenseArgs &a, float *
     }
   }
   if (__syncthreads_or(failed)) {
-    // Let copies still in flight land (bounded) before returning.
+    // Let copies still in flight land (bounded) before returning. A buffer
+    // is refilled only after every warp's wait for its previous copy
+    // succeeded, so at most its last issued copy is in flight: wait for
+    // that copy's phase. (The warps' `phase` bits also count the tiles they
+    // skipped after the failure, so they do not name it.)
     if (threadIdx.x == 0) {
-      for (int b2 = 0; b2 < NB; ++b2) mbar_wait_bounded(&ts->full[b2], (phase >> b2) & 1u, TILE_WAIT_LIMIT);
+      for (int b2 = 0; b2 < NB; ++b2)
+        if (ts->issued[b2]) mbar_wait_bounded(&ts->full[b2], (ts->issued[b2] - 1u) & 1u, TILE_WAIT_LIMIT);
       if (a.status) atomicExch(a.status, 1);
     }
     return false;
@@ -656,6 +667,7 @@ __device__ __forceinline__ void init_tile_sync(TileSync *ts) {
     for (int b = 0; b < TILE_MAX_BUFS; ++b) {
       mbar_init(&ts->full[b], 1);
       ts->done[b] = 0;
+      ts->issued[b] = 0;
     }
     ts->fail = 0;
     mbar_fence_init();
