@@ -286,3 +286,118 @@ def test_barrier_form_failure_path_drains_every_copy():
             failures += r["failed"]
             assert not r["missed"], (seed, total, r)
     assert failures > 50
+
+
+def run_ring_with_failures(S: int, n: int, seed: int, limit: int) -> dict:
+    """The tensor-core initial-field product's ring (sa_init.cu,
+    init_gemm_kernel): a copy thread loads chunk i into stage i mod S once
+    the MMAs released the stage's previous chunk (`empty`), an MMA thread
+    waits for each chunk (`full`), issues its MMAs and releases the stage
+    when they complete. Both waits are bounded; a thread whose wait runs out
+    stops. The copy thread then waits (bounded) on each stage's last copy,
+    the phase (last // S) of stage s with last = s + ((issued - 1 - s) // S) * S."""
+    rng = random.Random(seed)
+    full = [0] * S                 # landed copies per stage
+    empty = [0] * S                # released stages (MMAs completed)
+    copies = {}                    # stage -> (chunk, kind)
+    mmas = {}                      # stage -> (chunk, kind)
+    content = [None] * S
+    prod = {"i": 0, "polls": 0, "state": "run", "issued": 0, "drain_s": 0, "missed": []}
+    cons = {"i": 0, "polls": 0, "state": "run"}
+
+    def kind() -> str:
+        r = rng.random()
+        return "stuck" if r < 0.02 else "slow" if r < 0.08 else "normal"
+
+    def landable(d: dict, late: bool) -> list:
+        return [s for s, (_, k) in d.items() if k == "normal" or (k == "slow" and late)]
+
+    steps = 0
+    while prod["state"] != "done" or cons["state"] != "done":
+        steps += 1
+        assert steps < 100 * (n + S * limit) + 1000, "the ring stalled"
+        late = prod["state"] != "run" or cons["state"] != "run"
+        events = []
+        if landable(copies, late):
+            events.append("copy")
+        if landable(mmas, late):
+            events.append("mma")
+        if prod["state"] != "done":
+            events.append("prod")
+        if cons["state"] != "done":
+            events.append("cons")
+        if not events:                       # only stuck work left
+            break
+        e = rng.choice(events)
+        if e == "copy":
+            s = rng.choice(landable(copies, late))
+            content[s] = copies.pop(s)[0]
+            full[s] += 1
+        elif e == "mma":
+            s = rng.choice(landable(mmas, late))
+            mmas.pop(s)
+            empty[s] += 1
+        elif e == "prod":
+            if prod["state"] == "run":
+                i = prod["i"]
+                if i == n:
+                    prod["state"] = "drain"
+                    continue
+                s, u = i % S, i // S
+                if u > 0 and not _parity_done(empty[s], (u - 1) & 1):
+                    prod["polls"] += 1
+                    if prod["polls"] >= limit:
+                        prod["state"] = "drain"
+                    continue
+                prod["polls"] = 0
+                assert s not in copies, "two copies in flight in one stage"
+                copies[s] = (i, kind())
+                prod["i"] = i + 1
+                prod["issued"] = i + 1
+            else:                            # the drain, one stage at a time
+                s = prod["drain_s"]
+                issued = prod["issued"]
+                if s >= min(S, issued):
+                    prod["state"] = "done"
+                    continue
+                last = s + ((issued - 1 - s) // S) * S
+                assert full[s] in (last // S, last // S + 1), "the drain could confuse two phases"
+                if _parity_done(full[s], (last // S) & 1):
+                    if s in copies:
+                        prod["missed"].append(s)
+                    prod["drain_s"] += 1
+                    prod["polls"] = 0
+                else:
+                    prod["polls"] += 1
+                    if prod["polls"] >= limit:
+                        prod["drain_s"] += 1
+                        prod["polls"] = 0
+        else:
+            i = cons["i"]
+            if i == n or cons["state"] == "stop":
+                cons["state"] = "done"
+                continue
+            s, u = i % S, i // S
+            if not _parity_done(full[s], u & 1):
+                cons["polls"] += 1
+                if cons["polls"] >= limit:
+                    cons["state"] = "stop"
+                continue
+            cons["polls"] = 0
+            assert content[s] == i, f"MMA read chunk {content[s]} for chunk {i}"
+            assert s not in mmas
+            mmas[s] = (i, kind())
+            cons["i"] = i + 1
+    failed = prod["i"] < n or cons["i"] < n
+    return {"failed": failed, "missed": prod["missed"]}
+
+
+@pytest.mark.parametrize("S", [4, 6])
+def test_init_ring_failure_path_drains_every_copy(S):
+    failures = 0
+    for seed in range(400):
+        for n in (1, S - 1, S, S + 1, 12, 3 * S + 2):
+            r = run_ring_with_failures(S, n, seed, limit=6)
+            failures += r["failed"]
+            assert not r["missed"], (seed, n, r)
+    assert failures > 50
